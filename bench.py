@@ -1,0 +1,322 @@
+"""Benchmark: replica-exchange Monte Carlo throughput on one GB300.
+
+Metric (BASELINE): MC steps/s and residue-pair evaluations/s.  A bench "step" is one
+exchange block of the workload: every replica advances `--block` Monte Carlo steps
+(move, energy of the moved molecule, Metropolis) on the GPU, then one even/odd
+temperature exchange runs.  value = replica MC steps per second over the timed steps.
+
+Default workload: the flexible-linker configuration (76 + 10 + 76 residues, one
+chain, 32 replicas 288-450 K, flex moves 30 %), seeded synthetic inputs.  The
+state (a few hundred KB) lives in L2, so every timed step is preceded by an L2
+flush (a 256 MiB write) inside the timed region.
+
+Arms:
+  default            the GB300 engine (libcgppd_gb300.so), CUDA-graph replays
+  --impl reference   the reference CPU algorithm (full energy recomputation every
+                     step, reference precision) timed on this host's cores: the
+                     oracle's port of the reference loop, rank 0 only
+Launched with torchrun for N > 1, each rank runs an independent set of replicas
+("replicas only": the path has no cross-GPU exchange step), value = sum over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MC steps/s & pair-evals/s on 1 GB300: plain vs surrogate-screened, 1e-5 rel E"
+FLOP_PER_PAIR = 80  # 40 FP32-pipe ops (FMA-counted as 2 FLOP) per Kim-Hummer pair term
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="c1")
+    p.add_argument("--block", type=int, default=1000, help="MC steps per exchange block")
+    p.add_argument("--cluster", type=int, default=0)
+    p.add_argument("--threads", type=int, default=0)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU arm
+
+def cpu_port_rate(wl, seconds, threads):
+    """The oracle's port of the reference CPU loop on the workload's first simulation:
+    replica MC steps per second using `threads` host threads, on a bounded sample."""
+    from oracle.remc import OracleRemc
+    sim = wl.sims[0]
+    o = OracleRemc(sim.molecules, wl.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
+                   sim.move_weights, sim.rigid_rotate_prob, wl.torsion_V, wl.torsion_phase, seed=wl.seed)
+    R = o.R
+    t0 = time.perf_counter()
+    o.run(1, 2, threads=threads)
+    cal = max(time.perf_counter() - t0, 1e-4) / 2.0  # seconds per MC step of all replicas
+    steps = max(4, int(seconds / cal))
+    t0 = time.perf_counter()
+    o.run(1, steps, threads=threads)
+    dt = time.perf_counter() - t0
+    return R * steps / dt, steps, R, dt
+
+
+def reference_arm(args):
+    import cgppd_gb300.workloads as workloads
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = workloads.make(args.workload)
+    cores = os.cpu_count() or 1
+    sim = wl.sims[0]
+    threads = min(cores, len(sim.temperatures))
+    # one bench step = a bounded block of MC steps of all replicas
+    per = max(1.0, args.cpu_seconds / max(1, args.steps))
+    rates = []
+    for i in range(args.warmup + args.steps):
+        rate, steps, R, dt = cpu_port_rate(wl, per if i >= args.warmup else min(per, 2.0), threads)
+        if i >= args.warmup:
+            rates.append((rate, steps, dt))
+    total_steps = sum(r[0] * r[2] for r in rates)
+    total_t = sum(r[2] for r in rates)
+    value = total_steps / total_t
+    out = {"metric": METRIC, "impl": "reference", "value": value, "unit": "replica MC steps/s", "n_gpus": 0,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_t / len(rates),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64/fp32 (reference mix)",
+           "data": "synthetic (seeded, configuration shapes)",
+           "config": {"workload": wl.name, "replicas": len(sim.temperatures),
+                      "mc_steps_per_bench_step": [r[1] for r in rates]},
+           "cpu_baseline": {"value": value, "unit": "replica MC steps/s", "cores": threads, "kind": "port",
+                            "sample": "%d replicas x %s MC steps per bench step (full energy recomputation "
+                                      "each step, as the reference CPU path)" % (len(sim.temperatures),
+                                                                                 [r[1] for r in rates])},
+           "e2e": {"value": value, "unit": "replica MC steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def gpu_arm(args):
+    import torch
+    import cgppd_gb300
+    from cgppd_gb300 import engine as eng
+    from cgppd_gb300 import workloads
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    cgppd_gb300.lib()  # fails loudly if the library is missing
+
+    wl = workloads.make(args.workload, seed=None if rank == 0 else 20261203 + 1000 * rank + int(args.workload[1:]))
+    e = eng.from_workload(wl, cluster=args.cluster, threads=args.threads)
+    R = e.total_replicas
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    K = args.block
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            e.run(1, K, True, stream=sh)
+    barrier()
+    steps0, pairs0 = e.counters()
+    launches = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                e.run(1, K, True, stream=sh)
+                launches += e.last_launches()
+            ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    steps1, pairs1 = e.counters()
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    mc_steps = steps1 - steps0
+    pairs = pairs1 - pairs0
+    tot = torch.tensor([float(mc_steps), float(pairs)], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(tot)
+    value = tot[0].item() / (ms / 1000.0)
+    pair_rate = tot[1].item() / (ms / 1000.0)
+
+    # kernel-level timing of the MC block (the dominant kernel) with events on its stream
+    ktimes = []
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0 = e.counters()[1]
+            a.record(stream)
+            e.run(1, K, False, stream=sh)
+            b.record(stream)
+            b.synchronize()
+            ktimes.append((a.elapsed_time(b), e.counters()[1] - p0))
+    k_ms = float(np.mean([x[0] for x in ktimes]))
+    k_pairs = float(np.mean([x[1] for x in ktimes]))
+
+    # end to end through the public API with host buffers: upload every replica's state
+    # from pinned memory (with a fresh energy evaluation), run the block, download state
+    # and potentials, every step
+    e2e = None
+    if not args.no_e2e:
+        N, M, Rs = e.sim_info(0)
+        hp = torch.empty((Rs * N * 4,), dtype=torch.float32).pin_memory()
+        hr = torch.empty((Rs * N * 4,), dtype=torch.float32).pin_memory()
+        hc = torch.empty((Rs * M * 4,), dtype=torch.float32).pin_memory()
+        hpot = torch.empty((Rs,), dtype=torch.float64).pin_memory()
+        e.download(0, hp.data_ptr(), hr.data_ptr(), hc.data_ptr(), hpot.data_ptr(), stream=sh)
+        stream.synchronize()
+        n_e2e = max(2, args.steps // 2)
+        barrier()
+        t0 = time.perf_counter()
+        s0 = e.counters()[0]
+        for _ in range(n_e2e):
+            e.upload(0, hp.data_ptr(), hr.data_ptr(), hc.data_ptr(), recompute=True, stream=sh)
+            e.run(1, K, True, stream=sh)
+            e.download(0, hp.data_ptr(), hr.data_ptr(), hc.data_ptr(), hpot.data_ptr(), stream=sh)
+            stream.synchronize()
+        t1 = time.perf_counter()
+        done = e.counters()[0] - s0
+        h2d = (2 * Rs * N + Rs * M) * 16
+        d2h = h2d + Rs * 8
+        tt = torch.tensor([t1 - t0], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": done * world / float(tt.item()), "unit": "replica MC steps/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = min(os.cpu_count() or 1, len(wl.sims[0].temperatures))
+        rate, steps, Rr, dt = cpu_port_rate(wl, args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": "replica MC steps/s", "cores": threads, "kind": "port",
+               "sample": "%d replicas x %d MC steps of the same workload (%.1f s)" % (Rr, steps, dt)}
+
+    props = torch.cuda.get_device_properties(local)
+    clocks = clk.summary()
+    max_mhz = clocks["sm_max_mhz"] or 2070.0
+    peak_tflops = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
+    achieved = k_pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get(args.workload)
+        except ValueError:
+            traffic = None
+    shape = e.launch_shape()
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "replica MC steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded, configuration shapes)",
+            "config": {"workload": wl.name, "replicas": R, "mc_steps_per_bench_step": K,
+                       "exchange": "after every block", "l2": "256 MiB flush before every timed step, inside the "
+                                                             "timed region", "cluster_ctas_per_replica": shape[0],
+                       "threads_per_cta": shape[1], "parallelism": "replicas on one GPU" if world == 1 else
+                       "dp%d (independent replica sets)" % world},
+            "pair_evals_per_s": pair_rate,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+                         "frac": achieved / peak_tflops, "traffic": traffic,
+                         "kernel": "k_mc_block", "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,
+                         "flop_per_pair": FLOP_PER_PAIR,
+                         "peak_note": "nominal FP32 pipe: SMs x 128 lanes x 2 x max SM clock (no FP32 figure in "
+                                      "the measured peaks)"},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gpu_arm(a)

@@ -1,0 +1,942 @@
+// engine_host.cu -- host side of the batched replica-exchange engine (see cgppd_remc.h).
+//
+// Builds the device tables from molecules (flexible-segment graph, replica-wide
+// UIDs, exclusion keys, move candidate lists), owns the device buffers, and drives
+// the kernels as CUDA-graph replays of [MC block, exchange].
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <set>
+#include <vector>
+
+#include "cgppd_common.cuh"
+#include "cgppd_remc.h"
+#include "engine_types.h"
+#include "host/graph.h"
+#include "status.h"
+
+namespace cgppd {
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster);
+cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
+                            cudaStream_t stream);
+cudaError_t set_mc_smem_limit(size_t smem);
+cudaError_t launch_init_energy(const EngineArgs &a, int total_replicas, size_t smem, double *potential_out,
+                               cudaStream_t stream);
+cudaError_t launch_exchange(const EngineArgs &a, int nsims, int total_replicas, int steps_per_block,
+                            cudaStream_t stream);
+cudaError_t launch_final_report(const EngineArgs &a, int nsims, int total_replicas, int row, cudaStream_t stream);
+}  // namespace cgppd
+
+using namespace cgppd;
+
+namespace {
+
+struct HostMolecule {
+    int n = 0;
+    std::vector<float> xyz, rel;
+    float center[3] = {0, 0, 0};
+    std::vector<int> types, res_seq, chain_index;
+    std::vector<float> charges, radii;
+    std::vector<char> chain_ids;
+    int num_chains = 1;
+    bool all_flexible = false, crowder = false;
+    std::vector<std::vector<int>> segments;
+};
+
+struct HostSim {
+    cgppd_sim_params p{};
+    std::vector<float> temps, tsteps;
+    std::vector<double> rsteps;
+    std::vector<HostMolecule> mols;
+};
+
+template <typename T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count)
+    {
+        release();
+        n = std::max<size_t>(count, 1);
+        return cgppd_check(cudaMalloc(&ptr, n * sizeof(T)), "engine allocation");
+    }
+    int upload(const std::vector<T> &v)
+    {
+        if (alloc(v.size()) != 0)
+            return -1;
+        if (v.empty())
+            return cgppd_check(cudaMemset(ptr, 0, sizeof(T)), "engine memset");
+        return cgppd_check(cudaMemcpy(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "engine upload");
+    }
+    int zero(size_t count)
+    {
+        if (alloc(count) != 0)
+            return -1;
+        return cgppd_check(cudaMemset(ptr, 0, n * sizeof(T)), "engine memset");
+    }
+};
+
+
+}  // namespace
+
+struct cgppd_engine {
+    std::vector<float> table;  // Eij kcal, 32x32
+    std::vector<double> torsV, torsS;
+    int tors_types = 0;
+    int ntypes = 0;
+    uint64_t seed = 0;
+    std::vector<HostSim> sims;
+    bool finalized = false;
+
+    // launch shape
+    int cluster = 1, threads = 256;
+    size_t smem = 0;
+    int total_replicas = 0;
+    int max_n = 0, max_m = 0, max_mol = 0;
+    int report_capacity = 0;
+    int last_launches = 0;
+
+    cudaStream_t own_stream = nullptr;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, exchange) -> graph
+
+    // device buffers
+    DevBuf<DevSim> d_sims;
+    DevBuf<int> d_rep_sim;
+    DevBuf<DevMol> d_mols;
+    DevBuf<float4> d_rstat;
+    DevBuf<int4> d_rexcl;
+    DevBuf<int2> d_bonds, d_indsub;
+    DevBuf<int4> d_angles, d_tors, d_flexres, d_flexopt;
+    DevBuf<float4> d_torsV, d_torsS;
+    DevBuf<int> d_branch, d_localres, d_crankres;
+    DevBuf<float> d_table;
+    DevBuf<float4> d_pos, d_rel, d_center;
+    DevBuf<double> d_emat, d_intra, d_potential, d_scratch_pot, d_scratch_emat, d_scratch_intra;
+    DevBuf<float> d_temperature, d_tstep;
+    DevBuf<double> d_rstep;
+    DevBuf<unsigned long long> d_stepc, d_pairc;
+    DevBuf<ReplicaStats> d_stats;
+    DevBuf<int> d_tindex, d_label, d_slot_of_t, d_sim_state;
+    DevBuf<float4> d_report;
+    DevBuf<int2> d_exch_report;
+    DevBuf<unsigned> d_errflags;
+
+    std::vector<DevSim> h_sims;
+    std::vector<DevMol> h_mols;
+
+    ~cgppd_engine()
+    {
+        for (auto &kv : graphs)
+            cudaGraphExecDestroy(kv.second);
+        if (own_stream)
+            cudaStreamDestroy(own_stream);
+    }
+
+    EngineArgs args() const
+    {
+        EngineArgs a{};
+        a.sims = d_sims.ptr;
+        a.rep_sim = d_rep_sim.ptr;
+        a.mols = d_mols.ptr;
+        a.rstat = d_rstat.ptr;
+        a.rexcl = d_rexcl.ptr;
+        a.bonds = d_bonds.ptr;
+        a.angles = d_angles.ptr;
+        a.tors = d_tors.ptr;
+        a.torsV = d_torsV.ptr;
+        a.torsS = d_torsS.ptr;
+        a.indsub = d_indsub.ptr;
+        a.flexres = d_flexres.ptr;
+        a.flexopt = d_flexopt.ptr;
+        a.branch = d_branch.ptr;
+        a.localres = d_localres.ptr;
+        a.crankres = d_crankres.ptr;
+        a.table = d_table.ptr;
+        a.pos = d_pos.ptr;
+        a.rel = d_rel.ptr;
+        a.center = d_center.ptr;
+        a.emat = d_emat.ptr;
+        a.intra = d_intra.ptr;
+        a.potential = d_potential.ptr;
+        a.temperature = d_temperature.ptr;
+        a.tstep = d_tstep.ptr;
+        a.rstep = d_rstep.ptr;
+        a.stepc = d_stepc.ptr;
+        a.pairc = d_pairc.ptr;
+        a.stats = d_stats.ptr;
+        a.tindex = d_tindex.ptr;
+        a.label = d_label.ptr;
+        a.slot_of_t = d_slot_of_t.ptr;
+        a.sim_state = d_sim_state.ptr;
+        a.report = d_report.ptr;
+        a.exch_report = d_exch_report.ptr;
+        a.report_capacity = report_capacity;
+        a.errflags = d_errflags.ptr;
+        a.seed_lo = (uint32_t)seed;
+        a.seed_hi = (uint32_t)(seed >> 32);
+        a.ntypes = ntypes;
+        a.cluster = cluster;
+        a.max_n = max_n;
+        a.max_m = max_m;
+        a.max_mol = max_mol;
+        return a;
+    }
+
+    int build();
+};
+
+// Build every static table and the initial replica state.
+int cgppd_engine::build()
+{
+    std::vector<float4> rstat;
+    std::vector<int4> rexcl, angles, tors, flexres, flexopt;
+    std::vector<int2> bonds, indsub;
+    std::vector<float4> torsVv, torsSv;
+    std::vector<int> branch, localres, crankres, rep_sim;
+    std::vector<float4> pos, rel, center;
+    std::vector<float> temperature, tstep;
+    std::vector<double> rstep;
+    std::vector<int> tindex, label, slot_of_t;
+    const float qscale = std::sqrt(kDHFactor);
+    long long state_off = 0, emat_off = 0;
+    int molst_off = 0, rep_off = 0, res_off = 0, mol_off = 0;
+    h_sims.clear();
+    h_mols.clear();
+
+    for (size_t s = 0; s < sims.size(); ++s) {
+        HostSim &hs = sims[s];
+        DevSim ds{};
+        int N = 0;
+        for (auto &m : hs.mols)
+            N += m.n;
+        const int M = (int)hs.mols.size();
+        const int R = hs.p.n_replicas;
+        if (M == 0 || N == 0)
+            return cgppd_fail("engine: a simulation has no molecules");
+        if (!(hs.p.box > 0.0f))
+            return cgppd_fail("engine: the periodic box edge must be positive");
+        ds.N = N, ds.M = M, ds.R = R;
+        ds.res_off = res_off, ds.mol_off = mol_off, ds.rep_off = rep_off;
+        ds.state_off = state_off, ds.molst_off = molst_off, ds.emat_off = emat_off;
+        ds.box = hs.p.box, ds.inv_box = 1.0f / hs.p.box;
+        float wsum = 0.f;
+        for (int k = 0; k < 4; ++k)
+            wsum += hs.p.move_weights[k];
+        float acc = 0.f;
+        for (int k = 0; k < 4; ++k) {
+            acc += hs.p.move_weights[k];
+            ds.w_cum[k] = acc / wsum;
+        }
+        float w1 = hs.p.move_weights[1] + hs.p.move_weights[2] + hs.p.move_weights[3];
+        ds.w1_cum[0] = hs.p.move_weights[1] / w1;
+        ds.w1_cum[1] = (hs.p.move_weights[1] + hs.p.move_weights[2]) / w1;
+        ds.w1_cum[2] = 1.0f;
+        ds.rigid_rotate_p = hs.p.rigid_rotate_prob;
+        ds.sample_freq = hs.p.sample_frequency;
+        ds.sample_after = hs.p.sample_after;
+        ds.bound_threshold = hs.p.bound_threshold;
+
+        // replica-wide UIDs (Graph::assign_uids with running offsets, src/Replica.cpp:33-40)
+        int chain_off = 1, dom_off = 1, bond_off = 1;
+        int non_crowders = 0;
+        bool seen_crowder = false, flexible_exists = false;
+        int start = 0;
+        for (int mi = 0; mi < M; ++mi) {
+            HostMolecule &hm = hs.mols[mi];
+            const bool flexible = !hs.p.rigid_only && (hm.all_flexible || !hm.segments.empty());
+            flexible_exists = flexible_exists || (hm.all_flexible || !hm.segments.empty());
+            if (hm.crowder)
+                seen_crowder = true;
+            else if (!seen_crowder)
+                ++non_crowders;
+            Graph G;
+            G.init(hm.chain_ids, hm.all_flexible, hm.segments, hm.num_chains);
+            std::vector<int> chain_uid(hm.n, 0), dom_uid(hm.n, 0), bond_uid(hm.n, 0);
+            std::map<int, int> cu;
+            for (int c = 0; c < G.num_chains; ++c)
+                cu[c] = chain_off + c;
+            chain_off += G.num_chains;
+            for (size_t d = 0; d < G.rigid_domains.size(); ++d)
+                for (int v : G.rigid_domains[d])
+                    dom_uid[v] = dom_off + (int)d;
+            dom_off += (int)G.rigid_domains.size();
+            for (size_t b = 0; b < G.segment_bonds.size(); ++b) {
+                bond_uid[G.segment_bonds[b].i] = bond_off + (int)b;
+                bond_uid[G.segment_bonds[b].j] = bond_off + (int)b;
+            }
+            bond_off += (int)G.segment_bonds.size();
+            for (int i = 0; i < G.vertex_count() && i < hm.n; ++i) {
+                auto it = cu.find(hm.chain_index[i]);
+                chain_uid[i] = it == cu.end() ? 0 : it->second;
+            }
+            auto excluded = [&](int i, int j) {
+                return (dom_uid[i] && dom_uid[i] == dom_uid[j]) ||
+                       (chain_uid[i] == chain_uid[j] && std::abs(hm.res_seq[i] - hm.res_seq[j]) < 4) ||
+                       (bond_uid[i] && bond_uid[i] == bond_uid[j]);
+            };
+
+            DevMol dm{};
+            dm.start = start;
+            dm.count = hm.n;
+            dm.flags = (flexible ? kMolFlexible : 0) | (hm.crowder ? kMolCrowder : 0);
+            for (int i = 0; i < hm.n; ++i) {
+                float4 r4;
+                r4.x = 0.5f * hm.radii[i];
+                r4.y = hm.charges[i] * qscale;
+                int ty = hm.types[i];
+                if (ty < 0 || ty >= ntypes)
+                    return cgppd_fail("engine: residue type outside the contact table");
+                std::memcpy(&r4.z, &ty, 4);
+                int mol = mi;
+                std::memcpy(&r4.w, &mol, 4);
+                rstat.push_back(r4);
+                rexcl.push_back(make_int4(chain_uid[i], hm.res_seq[i], dom_uid[i], bond_uid[i]));
+            }
+            if (flexible) {
+                dm.bond_off = (int)bonds.size();
+                for (const auto &b : G.bonds)
+                    bonds.push_back(make_int2(b.i, b.j));
+                dm.nbond = (int)bonds.size() - dm.bond_off;
+                dm.ang_off = (int)angles.size();
+                for (const auto &an : G.angles)
+                    angles.push_back(make_int4(an.i, an.j, an.k, 0));
+                dm.nang = (int)angles.size() - dm.ang_off;
+                dm.tor_off = (int)tors.size();
+                for (const auto &t : G.torsions) {
+                    tors.push_back(make_int4(t.i, t.j, t.k, t.l));
+                    float4 V{0, 0, 0, 0}, S{0, 0, 0, 0};
+                    int a1 = hm.types[t.j], a2 = hm.types[t.k];
+                    if (!torsV.empty() && a1 < tors_types && a2 < tors_types) {
+                        const double *v = &torsV[4 * (a1 * tors_types + a2)];
+                        const double *sg = &torsS[4 * (a1 * tors_types + a2)];
+                        V = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+                        S = make_float4((float)sg[0], (float)sg[1], (float)sg[2], (float)sg[3]);
+                    }
+                    torsVv.push_back(V);
+                    torsSv.push_back(S);
+                }
+                dm.ntor = (int)tors.size() - dm.tor_off;
+                dm.ind_off = (int)indsub.size();
+                for (const auto &p : G.indirect_neighbours)
+                    if (!excluded(p.i, p.j))
+                        indsub.push_back(make_int2(p.i, p.j));
+                dm.nind = (int)indsub.size() - dm.ind_off;
+                long long nintra = 0;
+                for (int i = 0; i < hm.n; ++i)
+                    for (int j = i + 1; j < hm.n; ++j)
+                        if (!excluded(i, j) && !G.indirect_neighbours.count(Pair{i, j}))
+                            ++nintra;
+                dm.nintra = (int)nintra;
+                // flex candidates: branch of each (residue, neighbour) edge, extended by the
+                // other branches inside the residue's rigid domain (src/Molecule.cpp:331-360)
+                dm.flex_off = (int)flexres.size();
+                for (int ri : G.MC_flex_residues) {
+                    std::vector<int> nb = G.neighbours(ri);
+                    flexres.push_back(make_int4(ri, (int)nb.size(), (int)flexopt.size(), 0));
+                    std::set<int> dom = G.rigid_domain_around(ri);
+                    for (int nbr : nb) {
+                        std::set<int> br = G.branch(ri, nbr);
+                        if (dom.count(nbr))
+                            for (int other : nb)
+                                if (other != nbr && dom.count(other)) {
+                                    std::set<int> extra = G.branch(ri, other);
+                                    br.insert(extra.begin(), extra.end());
+                                }
+                        flexopt.push_back(make_int4(nbr, (int)branch.size(), (int)br.size(), 0));
+                        branch.insert(branch.end(), br.begin(), br.end());
+                    }
+                }
+                dm.nflex = (int)flexres.size() - dm.flex_off;
+                dm.local_off = (int)localres.size();
+                localres.insert(localres.end(), G.MC_local_residues.begin(), G.MC_local_residues.end());
+                dm.nlocal = (int)localres.size() - dm.local_off;
+                dm.crank_off = (int)crankres.size();
+                crankres.insert(crankres.end(), G.MC_crankshaft_residues.begin(), G.MC_crankshaft_residues.end());
+                dm.ncrank = (int)crankres.size() - dm.crank_off;
+            }
+            h_mols.push_back(dm);
+            start += hm.n;
+            max_mol = std::max(max_mol, hm.n);
+        }
+        ds.non_crowders = non_crowders;
+        // Replica::sample chooses what the bound test compares (src/Replica.cpp:1043-1075)
+        if (M == 1)
+            ds.nc_mode = 0;
+        else if (M != non_crowders || (flexible_exists && !hs.p.rigid_only))
+            ds.nc_mode = 1;
+        else
+            ds.nc_mode = 2;
+        ds.max_mol = 0;
+        for (auto &m : hs.mols)
+            ds.max_mol = std::max(ds.max_mol, m.n);
+
+        // replicas: every replica starts from the initial replica's coordinates
+        for (int r = 0; r < R; ++r) {
+            for (auto &hm : hs.mols)
+                for (int i = 0; i < hm.n; ++i) {
+                    pos.push_back(make_float4(hm.xyz[3 * i], hm.xyz[3 * i + 1], hm.xyz[3 * i + 2], 0.f));
+                    rel.push_back(make_float4(hm.rel[3 * i], hm.rel[3 * i + 1], hm.rel[3 * i + 2], 0.f));
+                }
+            for (auto &hm : hs.mols)
+                center.push_back(make_float4(hm.center[0], hm.center[1], hm.center[2], 0.f));
+            temperature.push_back(hs.temps[r]);
+            tstep.push_back(hs.tsteps[r]);
+            rstep.push_back(hs.rsteps[r]);
+            tindex.push_back(r);
+            label.push_back(r);
+            slot_of_t.push_back(r);
+            rep_sim.push_back((int)s);
+        }
+        h_sims.push_back(ds);
+        max_n = std::max(max_n, N);
+        max_m = std::max(max_m, M);
+        res_off += N;
+        mol_off += M;
+        rep_off += R;
+        state_off += (long long)N * R;
+        molst_off += M * R;
+        emat_off += (long long)M * M * R;
+    }
+    total_replicas = rep_off;
+    std::vector<int> sim_state(4 * sims.size(), 0);
+
+    int rc = 0;
+    rc |= d_sims.upload(h_sims);
+    rc |= d_rep_sim.upload(rep_sim);
+    rc |= d_mols.upload(h_mols);
+    rc |= d_rstat.upload(rstat);
+    rc |= d_rexcl.upload(rexcl);
+    rc |= d_bonds.upload(bonds);
+    rc |= d_indsub.upload(indsub);
+    rc |= d_angles.upload(angles);
+    rc |= d_tors.upload(tors);
+    rc |= d_torsV.upload(torsVv);
+    rc |= d_torsS.upload(torsSv);
+    rc |= d_flexres.upload(flexres);
+    rc |= d_flexopt.upload(flexopt);
+    rc |= d_branch.upload(branch);
+    rc |= d_localres.upload(localres);
+    rc |= d_crankres.upload(crankres);
+    rc |= d_table.upload(table);
+    rc |= d_pos.upload(pos);
+    rc |= d_rel.upload(rel);
+    rc |= d_center.upload(center);
+    rc |= d_emat.zero((size_t)emat_off);
+    rc |= d_intra.zero((size_t)molst_off);
+    rc |= d_potential.zero((size_t)total_replicas);
+    rc |= d_scratch_pot.zero((size_t)total_replicas);
+    rc |= d_temperature.upload(temperature);
+    rc |= d_tstep.upload(tstep);
+    rc |= d_rstep.upload(rstep);
+    rc |= d_stepc.zero((size_t)total_replicas);
+    rc |= d_pairc.zero((size_t)total_replicas);
+    rc |= d_stats.zero((size_t)total_replicas);
+    rc |= d_tindex.upload(tindex);
+    rc |= d_label.upload(label);
+    rc |= d_slot_of_t.upload(slot_of_t);
+    rc |= d_sim_state.upload(sim_state);
+    rc |= d_errflags.zero((size_t)total_replicas);
+    report_capacity = 0;
+    return rc ? -1 : 0;
+}
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+cgppd_engine *cgppd_engine_create(const float *lj_raw, int ntypes, const double *torsion_V,
+                                  const double *torsion_phase, int torsion_types, uint64_t seed)
+{
+    if (lj_raw == nullptr || ntypes <= 0 || ntypes > 32) {
+        cgppd_fail("cgppd_engine_create: the contact table must have 1..32 types");
+        return nullptr;
+    }
+    auto *e = new cgppd_engine();
+    e->ntypes = ntypes;
+    e->seed = seed;
+    e->table.assign(32 * 32, 0.0f);
+    // Eij = lambda (e_ij - e0) in RT units, as the reference forms it in float
+    // (src/Potential.cpp:14), then in kcal/mol.
+    for (int i = 0; i < ntypes; ++i)
+        for (int j = 0; j < ntypes; ++j)
+            e->table[i * 32 + j] = (kLambda * (lj_raw[i * ntypes + j] - kE0)) * kRTtoKcal;
+    if (torsion_V && torsion_phase && torsion_types > 0) {
+        e->tors_types = torsion_types;
+        e->torsV.assign(torsion_V, torsion_V + 4 * torsion_types * torsion_types);
+        e->torsS.assign(torsion_phase, torsion_phase + 4 * torsion_types * torsion_types);
+    }
+    return e;
+}
+
+void cgppd_engine_destroy(cgppd_engine *e) { delete e; }
+
+int cgppd_engine_add_simulation(cgppd_engine *e, const cgppd_sim_params *p)
+{
+    if (e->finalized)
+        return cgppd_fail("cgppd_engine_add_simulation: engine already finalized");
+    if (p->n_replicas <= 0 || !p->temperatures || !p->translate_steps || !p->rotate_steps)
+        return cgppd_fail("cgppd_engine_add_simulation: replica ladders are required");
+    HostSim hs;
+    hs.p = *p;
+    hs.temps.assign(p->temperatures, p->temperatures + p->n_replicas);
+    hs.tsteps.assign(p->translate_steps, p->translate_steps + p->n_replicas);
+    hs.rsteps.assign(p->rotate_steps, p->rotate_steps + p->n_replicas);
+    hs.p.temperatures = nullptr;
+    hs.p.translate_steps = nullptr;
+    hs.p.rotate_steps = nullptr;
+    e->sims.push_back(hs);
+    return (int)e->sims.size() - 1;
+}
+
+int cgppd_engine_add_molecule(cgppd_engine *e, int sim, int n, const float *xyz, const int *types,
+                              const float *charges, const float *radii, const char *chain_ids,
+                              const int *res_seq, const int *chain_index, int num_chains, int all_flexible,
+                              int crowder, int n_segments, const int *seg_lengths, const int *seg_residues,
+                              const float *center)
+{
+    if (e->finalized || sim < 0 || sim >= (int)e->sims.size() || n <= 0)
+        return cgppd_fail("cgppd_engine_add_molecule: bad arguments");
+    HostMolecule m;
+    m.n = n;
+    m.xyz.assign(xyz, xyz + 3 * n);
+    m.types.assign(types, types + n);
+    m.charges.assign(charges, charges + n);
+    m.radii.assign(radii, radii + n);
+    m.chain_ids.assign(chain_ids, chain_ids + n);
+    m.res_seq.assign(res_seq, res_seq + n);
+    m.chain_index.assign(chain_index, chain_index + n);
+    m.num_chains = num_chains > 0 ? num_chains : 1;
+    m.all_flexible = all_flexible != 0;
+    m.crowder = crowder != 0;
+    int off = 0;
+    for (int k = 0; k < n_segments; ++k) {
+        std::vector<int> seg(seg_residues + off, seg_residues + off + seg_lengths[k]);
+        for (int v : seg)
+            if (v < 0 || v >= n)
+                return cgppd_fail("cgppd_engine_add_molecule: segment residue out of range");
+        m.segments.push_back(seg);
+        off += seg_lengths[k];
+    }
+    if (center) {
+        std::memcpy(m.center, center, sizeof(m.center));
+    } else {
+        // float accumulation then division, as Molecule::initFromPDB (src/Molecule.cpp:590-604)
+        float c[3] = {0, 0, 0};
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k)
+                c[k] += xyz[3 * i + k];
+        for (int k = 0; k < 3; ++k)
+            m.center[k] = c[k] / (float)n;
+    }
+    m.rel.resize(3 * n);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k)
+            m.rel[3 * i + k] = xyz[3 * i + k] - m.center[k];
+    e->sims[sim].mols.push_back(m);
+    return (int)e->sims[sim].mols.size() - 1;
+}
+
+int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
+{
+    if (e->finalized)
+        return 0;
+    if (e->sims.empty())
+        return cgppd_fail("cgppd_engine_finalize: no simulation");
+    if (e->build() != 0)
+        return -1;
+    e->threads = (threads == 128) ? 128 : 256;
+    if (cluster <= 0) {
+        // enough CTAs to cover the SMs at least once when replicas are few
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cluster = 1;
+        while (cluster < 8 && e->total_replicas * cluster < sms && e->max_n / (cluster * 2) >= e->threads / 4)
+            cluster *= 2;
+    }
+    e->cluster = std::min(8, std::max(1, cluster));
+    const size_t s_mc = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, e->cluster);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1);
+    e->smem = s_mc;
+    if (std::max(s_mc, s_init) > 227 * 1024)
+        return cgppd_fail("cgppd_engine_finalize: system too large for shared memory (reduce molecule size or N)");
+    if (cgppd_check(set_mc_smem_limit(std::max(s_mc, s_init)), "engine shared-memory limit") != 0)
+        return -1;
+    if (cgppd_check(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking), "engine stream") != 0)
+        return -1;
+    EngineArgs a = e->args();
+    if (cgppd_check(launch_init_energy(a, e->total_replicas, s_init, e->d_potential.ptr, e->own_stream),
+                    "initial energy") != 0)
+        return -1;
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "initial energy") != 0)
+        return -1;
+    e->finalized = true;
+    return 0;
+}
+
+static int ensure_reports(cgppd_engine *e, int rows)
+{
+    if (rows <= e->report_capacity)
+        return 0;
+    // keep existing rows
+    const int cap = std::max(rows, 2 * e->report_capacity);
+    DevBuf<float4> nr;
+    DevBuf<int2> ne;
+    if (nr.zero((size_t)cap * e->total_replicas) != 0 || ne.zero((size_t)cap * e->sims.size()) != 0)
+        return -1;
+    if (e->report_capacity > 0) {
+        cudaMemcpy(nr.ptr, e->d_report.ptr, sizeof(float4) * (size_t)e->report_capacity * e->total_replicas,
+                   cudaMemcpyDeviceToDevice);
+        cudaMemcpy(ne.ptr, e->d_exch_report.ptr, sizeof(int2) * (size_t)e->report_capacity * e->sims.size(),
+                   cudaMemcpyDeviceToDevice);
+    }
+    std::swap(e->d_report.ptr, nr.ptr);
+    std::swap(e->d_report.n, nr.n);
+    std::swap(e->d_exch_report.ptr, ne.ptr);
+    std::swap(e->d_exch_report.n, ne.n);
+    e->report_capacity = cap;
+    for (auto &kv : e->graphs)  // graphs captured the old buffer pointers
+        cudaGraphExecDestroy(kv.second);
+    e->graphs.clear();
+    return 0;
+}
+
+static int exchanges_done(cgppd_engine *e)
+{
+    int st[4] = {0, 0, 0, 0};
+    cudaMemcpy(st, e->d_sim_state.ptr, sizeof(st), cudaMemcpyDeviceToHost);
+    return st[1];
+}
+
+int cgppd_engine_run(cgppd_engine *e, int n_blocks, int steps_per_block, int exchange_after_last, void *stream)
+{
+    if (!e->finalized)
+        return cgppd_fail("cgppd_engine_run: engine not finalized");
+    if (n_blocks <= 0 || steps_per_block <= 0)
+        return 0;
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->own_stream;
+    // report rows: one per exchange (+1 for a closing report)
+    const int need = exchanges_done(e) + n_blocks + 1;
+    if (ensure_reports(e, need) != 0)
+        return -1;
+    EngineArgs a = e->args();
+    const int nsims = (int)e->sims.size();
+    int launches = 0;
+    for (int b = 0; b < n_blocks; ++b) {
+        const bool exch = (b + 1 < n_blocks) || exchange_after_last;
+        const auto key = std::make_pair(steps_per_block, exch ? 1 : 0);
+        auto it = e->graphs.find(key);
+        if (it == e->graphs.end()) {
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            if (cgppd_check(cudaStreamBeginCapture(e->own_stream, cudaStreamCaptureModeThreadLocal), "capture") != 0)
+                return -1;
+            cudaError_t err = launch_mc_block(a, e->total_replicas, steps_per_block, e->threads, e->smem, e->own_stream);
+            if (err == cudaSuccess && exch)
+                err = launch_exchange(a, nsims, e->total_replicas, steps_per_block, e->own_stream);
+            cudaError_t err2 = cudaStreamEndCapture(e->own_stream, &g);
+            if (cgppd_check(err, "MC block launch") != 0 || cgppd_check(err2, "end capture") != 0)
+                return -1;
+            if (cgppd_check(cudaGraphInstantiate(&ge, g, 0), "graph instantiate") != 0)
+                return -1;
+            cudaGraphDestroy(g);
+            it = e->graphs.emplace(key, ge).first;
+        }
+        if (cgppd_check(cudaGraphLaunch(it->second, st), "graph launch") != 0)
+            return -1;
+        launches += exch ? 2 : 1;
+    }
+    e->last_launches = launches;
+    return 0;
+}
+
+int cgppd_engine_final_report(cgppd_engine *e, int row, void *stream)
+{
+    if (ensure_reports(e, row + 1) != 0)
+        return -1;
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->own_stream;
+    return cgppd_check(launch_final_report(e->args(), (int)e->sims.size(), e->total_replicas, row, st),
+                       "final report");
+}
+
+int cgppd_engine_synchronize(cgppd_engine *e)
+{
+    int rc = cgppd_check(cudaStreamSynchronize(e->own_stream), "engine synchronize");
+    if (rc == 0)
+        rc = cgppd_check(cudaDeviceSynchronize(), "engine synchronize");
+    return rc;
+}
+
+int cgppd_engine_total_replicas(const cgppd_engine *e) { return e->total_replicas; }
+
+int cgppd_engine_sim_info(const cgppd_engine *e, int sim, int *n_residues, int *n_molecules, int *n_replicas)
+{
+    if (sim < 0 || sim >= (int)e->sims.size())
+        return cgppd_fail("cgppd_engine_sim_info: bad simulation index");
+    int N = 0;
+    for (auto &m : e->sims[sim].mols)
+        N += m.n;
+    if (n_residues)
+        *n_residues = N;
+    if (n_molecules)
+        *n_molecules = (int)e->sims[sim].mols.size();
+    if (n_replicas)
+        *n_replicas = e->sims[sim].p.n_replicas;
+    return 0;
+}
+
+int cgppd_engine_recompute(cgppd_engine *e, double *out, int write_state)
+{
+    if (!e->finalized)
+        return cgppd_fail("cgppd_engine_recompute: engine not finalized");
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "recompute") != 0)
+        return -1;
+    EngineArgs a = e->args();
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1);
+    double *dst = write_state ? e->d_potential.ptr : e->d_scratch_pot.ptr;
+    if (!write_state) {
+        // evaluate into scratch copies so the running state is untouched
+        if (e->d_scratch_emat.n < e->d_emat.n && e->d_scratch_emat.zero(e->d_emat.n) != 0)
+            return -1;
+        if (e->d_scratch_intra.n < e->d_intra.n && e->d_scratch_intra.zero(e->d_intra.n) != 0)
+            return -1;
+        a.emat = e->d_scratch_emat.ptr;
+        a.intra = e->d_scratch_intra.ptr;
+    }
+    if (cgppd_check(launch_init_energy(a, e->total_replicas, s_init, dst, e->own_stream), "recompute") != 0)
+        return -1;
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "recompute") != 0)
+        return -1;
+    if (out)
+        return cgppd_check(cudaMemcpy(out, dst, sizeof(double) * e->total_replicas, cudaMemcpyDeviceToHost),
+                           "recompute copy");
+    return 0;
+}
+
+int cgppd_engine_get_replicas(cgppd_engine *e, int sim, double *potentials, float *temperatures, int *labels,
+                              int *tindex, int *stats16)
+{
+    if (sim < 0 || sim >= (int)e->h_sims.size())
+        return cgppd_fail("cgppd_engine_get_replicas: bad simulation index");
+    cudaDeviceSynchronize();
+    const DevSim &S = e->h_sims[sim];
+    int rc = 0;
+    if (potentials)
+        rc |= cgppd_check(cudaMemcpy(potentials, e->d_potential.ptr + S.rep_off, sizeof(double) * S.R,
+                                     cudaMemcpyDeviceToHost), "copy");
+    if (temperatures)
+        rc |= cgppd_check(cudaMemcpy(temperatures, e->d_temperature.ptr + S.rep_off, sizeof(float) * S.R,
+                                     cudaMemcpyDeviceToHost), "copy");
+    if (labels)
+        rc |= cgppd_check(cudaMemcpy(labels, e->d_label.ptr + S.rep_off, sizeof(int) * S.R, cudaMemcpyDeviceToHost),
+                          "copy");
+    if (tindex)
+        rc |= cgppd_check(cudaMemcpy(tindex, e->d_tindex.ptr + S.rep_off, sizeof(int) * S.R, cudaMemcpyDeviceToHost),
+                          "copy");
+    if (stats16) {
+        static_assert(sizeof(ReplicaStats) == 64, "ReplicaStats is 16 words");
+        rc |= cgppd_check(cudaMemcpy(stats16, e->d_stats.ptr + S.rep_off, sizeof(ReplicaStats) * S.R,
+                                     cudaMemcpyDeviceToHost), "copy");
+    }
+    return rc ? -1 : 0;
+}
+
+int cgppd_engine_get_state(cgppd_engine *e, int sim, int replica, float *xyz, float *rel, float *centers)
+{
+    if (sim < 0 || sim >= (int)e->h_sims.size() || replica < 0 || replica >= e->h_sims[sim].R)
+        return cgppd_fail("cgppd_engine_get_state: bad index");
+    cudaDeviceSynchronize();
+    const DevSim &S = e->h_sims[sim];
+    std::vector<float4> buf(std::max(S.N, S.M));
+    const long long off = S.state_off + (long long)replica * S.N;
+    if (xyz) {
+        if (cgppd_check(cudaMemcpy(buf.data(), e->d_pos.ptr + off, sizeof(float4) * S.N, cudaMemcpyDeviceToHost),
+                        "copy") != 0)
+            return -1;
+        for (int i = 0; i < S.N; ++i)
+            xyz[3 * i] = buf[i].x, xyz[3 * i + 1] = buf[i].y, xyz[3 * i + 2] = buf[i].z;
+    }
+    if (rel) {
+        if (cgppd_check(cudaMemcpy(buf.data(), e->d_rel.ptr + off, sizeof(float4) * S.N, cudaMemcpyDeviceToHost),
+                        "copy") != 0)
+            return -1;
+        for (int i = 0; i < S.N; ++i)
+            rel[3 * i] = buf[i].x, rel[3 * i + 1] = buf[i].y, rel[3 * i + 2] = buf[i].z;
+    }
+    if (centers) {
+        if (cgppd_check(cudaMemcpy(buf.data(), e->d_center.ptr + S.molst_off + (long long)replica * S.M,
+                                   sizeof(float4) * S.M, cudaMemcpyDeviceToHost), "copy") != 0)
+            return -1;
+        for (int m = 0; m < S.M; ++m)
+            centers[3 * m] = buf[m].x, centers[3 * m + 1] = buf[m].y, centers[3 * m + 2] = buf[m].z;
+    }
+    return 0;
+}
+
+int cgppd_engine_set_state(cgppd_engine *e, int sim, int replica, const float *xyz, const float *rel,
+                           const float *centers)
+{
+    if (sim < 0 || sim >= (int)e->h_sims.size() || replica < 0 || replica >= e->h_sims[sim].R)
+        return cgppd_fail("cgppd_engine_set_state: bad index");
+    const DevSim &S = e->h_sims[sim];
+    std::vector<float4> buf(std::max(S.N, S.M));
+    const long long off = S.state_off + (long long)replica * S.N;
+    int rc = 0;
+    if (xyz) {
+        for (int i = 0; i < S.N; ++i)
+            buf[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.f);
+        rc |= cgppd_check(cudaMemcpy(e->d_pos.ptr + off, buf.data(), sizeof(float4) * S.N, cudaMemcpyHostToDevice),
+                          "copy");
+    }
+    if (rel) {
+        for (int i = 0; i < S.N; ++i)
+            buf[i] = make_float4(rel[3 * i], rel[3 * i + 1], rel[3 * i + 2], 0.f);
+        rc |= cgppd_check(cudaMemcpy(e->d_rel.ptr + off, buf.data(), sizeof(float4) * S.N, cudaMemcpyHostToDevice),
+                          "copy");
+    }
+    if (centers) {
+        for (int m = 0; m < S.M; ++m)
+            buf[m] = make_float4(centers[3 * m], centers[3 * m + 1], centers[3 * m + 2], 0.f);
+        rc |= cgppd_check(cudaMemcpy(e->d_center.ptr + S.molst_off + (long long)replica * S.M, buf.data(),
+                                     sizeof(float4) * S.M, cudaMemcpyHostToDevice), "copy");
+    }
+    return rc ? -1 : 0;
+}
+
+int cgppd_engine_upload(cgppd_engine *e, int sim, const float *pos4, const float *rel4, const float *centers4,
+                        int recompute, void *stream)
+{
+    if (!e->finalized || sim < 0 || sim >= (int)e->h_sims.size())
+        return cgppd_fail("cgppd_engine_upload: bad simulation index");
+    const DevSim &S = e->h_sims[sim];
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->own_stream;
+    const size_t nres = (size_t)S.N * S.R;
+    int rc = 0;
+    if (pos4)
+        rc |= cgppd_check(cudaMemcpyAsync(e->d_pos.ptr + S.state_off, pos4, sizeof(float4) * nres,
+                                          cudaMemcpyHostToDevice, st), "upload positions");
+    if (rel4)
+        rc |= cgppd_check(cudaMemcpyAsync(e->d_rel.ptr + S.state_off, rel4, sizeof(float4) * nres,
+                                          cudaMemcpyHostToDevice, st), "upload relative positions");
+    if (centers4)
+        rc |= cgppd_check(cudaMemcpyAsync(e->d_center.ptr + S.molst_off, centers4, sizeof(float4) * S.M * S.R,
+                                          cudaMemcpyHostToDevice, st), "upload centres");
+    if (rc == 0 && recompute) {
+        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1);
+        rc |= cgppd_check(launch_init_energy(e->args(), e->total_replicas, s_init, e->d_potential.ptr, st),
+                          "upload recompute");
+    }
+    return rc ? -1 : 0;
+}
+
+int cgppd_engine_download(cgppd_engine *e, int sim, float *pos4, float *rel4, float *centers4, double *potentials,
+                          void *stream)
+{
+    if (!e->finalized || sim < 0 || sim >= (int)e->h_sims.size())
+        return cgppd_fail("cgppd_engine_download: bad simulation index");
+    const DevSim &S = e->h_sims[sim];
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->own_stream;
+    const size_t nres = (size_t)S.N * S.R;
+    int rc = 0;
+    if (pos4)
+        rc |= cgppd_check(cudaMemcpyAsync(pos4, e->d_pos.ptr + S.state_off, sizeof(float4) * nres,
+                                          cudaMemcpyDeviceToHost, st), "download positions");
+    if (rel4)
+        rc |= cgppd_check(cudaMemcpyAsync(rel4, e->d_rel.ptr + S.state_off, sizeof(float4) * nres,
+                                          cudaMemcpyDeviceToHost, st), "download relative positions");
+    if (centers4)
+        rc |= cgppd_check(cudaMemcpyAsync(centers4, e->d_center.ptr + S.molst_off, sizeof(float4) * S.M * S.R,
+                                          cudaMemcpyDeviceToHost, st), "download centres");
+    if (potentials)
+        rc |= cgppd_check(cudaMemcpyAsync(potentials, e->d_potential.ptr + S.rep_off, sizeof(double) * S.R,
+                                          cudaMemcpyDeviceToHost, st), "download potentials");
+    return rc ? -1 : 0;
+}
+
+int cgppd_engine_get_matrix(cgppd_engine *e, int sim, int replica, double *E, double *intra)
+{
+    if (sim < 0 || sim >= (int)e->h_sims.size() || replica < 0 || replica >= e->h_sims[sim].R)
+        return cgppd_fail("cgppd_engine_get_matrix: bad index");
+    cudaDeviceSynchronize();
+    const DevSim &S = e->h_sims[sim];
+    int rc = 0;
+    if (E)
+        rc |= cgppd_check(cudaMemcpy(E, e->d_emat.ptr + S.emat_off + (long long)replica * S.M * S.M,
+                                     sizeof(double) * S.M * S.M, cudaMemcpyDeviceToHost), "copy");
+    if (intra)
+        rc |= cgppd_check(cudaMemcpy(intra, e->d_intra.ptr + S.molst_off + (long long)replica * S.M,
+                                     sizeof(double) * S.M, cudaMemcpyDeviceToHost), "copy");
+    return rc ? -1 : 0;
+}
+
+int cgppd_engine_get_report(cgppd_engine *e, int sim, int row, float *per_temperature4, int *exch2)
+{
+    if (sim < 0 || sim >= (int)e->h_sims.size() || row < 0 || row >= e->report_capacity)
+        return cgppd_fail("cgppd_engine_get_report: bad index");
+    cudaDeviceSynchronize();
+    const DevSim &S = e->h_sims[sim];
+    int rc = 0;
+    if (per_temperature4)
+        rc |= cgppd_check(cudaMemcpy(per_temperature4, e->d_report.ptr + (long long)row * e->total_replicas + S.rep_off,
+                                     sizeof(float4) * S.R, cudaMemcpyDeviceToHost), "copy");
+    if (exch2)
+        rc |= cgppd_check(cudaMemcpy(exch2, e->d_exch_report.ptr + (long long)row * e->sims.size() + sim, sizeof(int2),
+                                     cudaMemcpyDeviceToHost), "copy");
+    return rc ? -1 : 0;
+}
+
+int cgppd_engine_counters(cgppd_engine *e, unsigned long long *mc_steps, unsigned long long *pair_evals)
+{
+    cudaDeviceSynchronize();
+    std::vector<unsigned long long> a(e->total_replicas), b(e->total_replicas);
+    if (cgppd_check(cudaMemcpy(a.data(), e->d_stepc.ptr, sizeof(unsigned long long) * a.size(), cudaMemcpyDeviceToHost),
+                    "copy") != 0 ||
+        cgppd_check(cudaMemcpy(b.data(), e->d_pairc.ptr, sizeof(unsigned long long) * b.size(), cudaMemcpyDeviceToHost),
+                    "copy") != 0)
+        return -1;
+    unsigned long long sa = 0, sb = 0;
+    for (size_t i = 0; i < a.size(); ++i)
+        sa += a[i], sb += b[i];
+    if (mc_steps)
+        *mc_steps = sa;
+    if (pair_evals)
+        *pair_evals = sb;
+    return 0;
+}
+
+unsigned cgppd_engine_error_bits(cgppd_engine *e)
+{
+    cudaDeviceSynchronize();
+    std::vector<unsigned> f(e->total_replicas);
+    cudaMemcpy(f.data(), e->d_errflags.ptr, sizeof(unsigned) * f.size(), cudaMemcpyDeviceToHost);
+    unsigned o = 0;
+    for (unsigned v : f)
+        o |= v;
+    return o;
+}
+
+int cgppd_engine_last_launches(const cgppd_engine *e) { return e->last_launches; }
+
+int cgppd_engine_launch_shape(const cgppd_engine *e, int *cluster, int *threads)
+{
+    if (cluster)
+        *cluster = e->cluster;
+    if (threads)
+        *threads = e->threads;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,1057 @@
+// engine_kernels.cu -- device side of the batched replica-exchange Monte Carlo engine.
+//
+// k_mc_block: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
+// that replica with no inter-replica traffic (replicas are independent between
+// exchanges).  A step restates Replica::MCSearch (src/Replica.cpp:350-414):
+//   1. pick a molecule and a move (src/Molecule.cpp:451-504) from Philox draws,
+//   2. build the moved molecule's proposed coordinates in shared memory,
+//   3. evaluate the moved molecule against every other residue (its row of the
+//      molecule-pair energy matrix) and, for a flexible molecule, its internal
+//      non-bonded + bonded energy (src/Molecule.cpp:636-699),
+//   4. new total = old total - old row + new row; Metropolis on the float delta with
+//      the float Boltzmann factor, as the reference does (src/Replica.cpp:385-410),
+//   5. on accept, commit coordinates and the row (copy-on-accept; nothing to undo).
+// The reference recomputes every pair each step; only the moved molecule's pairs
+// change, so the engine evaluates those and keeps the rest in the matrix.
+//
+// Within a cluster every CTA builds the same proposal (same draws, same arithmetic),
+// takes a slice of the other residues, and the per-molecule partial rows are summed
+// through distributed shared memory in a fixed order, so all CTAs take the same
+// Metropolis decision.  CTA rank 0 alone writes global state.
+//
+// k_exchange: one warp per simulation performs the even/odd temperature exchange of
+// Simulation::run (src/Simulation.cpp:770-795) and the per-temperature bookkeeping of
+// Replica::fraction_bound / acceptance_ratio (src/Replica.cpp:1095-1122).
+#include <cooperative_groups.h>
+
+#include "cgppd_common.cuh"
+#include "engine_types.h"
+
+namespace cg = cooperative_groups;
+
+namespace cgppd {
+
+constexpr int kTableStride = 32;
+
+struct MoveDesc {
+    int m, start, n, type, kind;
+    int ri, br_off, br_cnt;
+    int flexible, wrapped, null_move;
+    float R[9];
+    float vx, vy, vz;        // translation of the molecule (translate) or of residue ri (local)
+    float fx, fy, fz;        // v / n (local translate)
+    float cx, cy, cz;        // centre before the move
+    float wcx, wcy, wcz;     // centre after the move (wrapped)
+    float px, py, pz;        // flex pivot position
+    double u_metro;
+};
+
+struct SmemLayout {
+    // byte offsets into dynamic shared memory
+    int table, ipos, irel, iq, iexcl, idisp, ej, rowp, row, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int max_m)
+{
+    SmemLayout L;
+    int off = 0;
+    L.table = off; off += kTableStride * kTableStride * 4;
+    L.ipos = off;  off += 16 * max_mol;
+    L.irel = off;  off += 16 * max_mol;
+    L.iexcl = off; off += 16 * max_mol;
+    L.idisp = off; off += 16 * max_mol;
+    L.iq = off;    off += 8 * max_mol;
+    L.ej = off;    off += 8 * slice;
+    off = (off + 7) & ~7;
+    L.rowp = off;  off += 8 * (max_m + 1);
+    L.row = off;   off += 8 * (max_m + 1);
+    L.total = off;
+    return L;
+}
+
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster)
+{
+    int slice = (max_n + cluster - 1) / cluster;
+    return (size_t)smem_layout(max_mol, slice, max_m).total;
+}
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ FF ff_make(float hi, float lo) { return FF{hi, lo}; }
+
+__device__ __forceinline__ void ff_add_ff(FF &a, FF b)
+{
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float err = (a.hi - (s - bb)) + (b.hi - bb);
+    a.hi = s;
+    a.lo += err + b.lo;
+}
+
+__device__ __forceinline__ FF ff_warp_sum(FF v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        FF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        ff_add_ff(v, w);
+    }
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide double sum in a fixed order; result valid in every thread.
+__device__ double block_sum_d(double v, double *red)
+{
+    const int t = threadIdx.x, nw = blockDim.x >> 5;
+    v = warp_sum_d(v);
+    __syncthreads();
+    if ((t & 31) == 0)
+        red[t >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w)
+        s += red[w];
+    return s;
+}
+
+__device__ __forceinline__ float3 rot_apply(const float *R, float x, float y, float z)
+{
+    return make_float3(fmaf(R[0], x, fmaf(R[1], y, R[2] * z)), fmaf(R[3], x, fmaf(R[4], y, R[5] * z)),
+                       fmaf(R[6], x, fmaf(R[7], y, R[8] * z)));
+}
+
+// Rotation matrix of quaternion (w, x, y, z), coefficients in double as
+// Quaternion::rotateVector forms them (src/Quaternion.cpp:95-112), stored as float.
+__device__ void quat_to_matrix(double w, double x, double y, double z, float *R)
+{
+    double w2 = w * w, x2 = x * x, y2 = y * y, z2 = z * z;
+    double wx = w * x, wy = w * y, wz = w * z, xy = x * y, xz = x * z, yz = y * z;
+    R[0] = (float)(w2 + x2 - y2 - z2);
+    R[1] = (float)((xy - wz) * 2.0);
+    R[2] = (float)((wy + xz) * 2.0);
+    R[3] = (float)((wz + xy) * 2.0);
+    R[4] = (float)(w2 - x2 + y2 - z2);
+    R[5] = (float)((yz - wx) * 2.0);
+    R[6] = (float)((xz - wy) * 2.0);
+    R[7] = (float)((yz + wx) * 2.0);
+    R[8] = (float)(w2 - x2 - y2 + z2);
+}
+
+// Quaternion(angle, axis) (src/Quaternion.cpp:12-21), optionally normalised
+// (Quaternion::normalize, :30-38), into a rotation matrix.
+__device__ void axis_angle_matrix(double angle, double ax, double ay, double az, bool normalize, float *R)
+{
+    double s, c;
+    sincos(angle / 2.0, &s, &c);
+    double w = c, x = s * ax, y = s * ay, z = s * az;
+    if (normalize) {
+        double mag = sqrt(w * w + x * x + y * y + z * z);
+        w /= mag;
+        x /= mag;
+        y /= mag;
+        z /= mag;
+    }
+    quat_to_matrix(w, x, y, z, R);
+}
+
+// Molecule::wrapped_centre: fmod per component (keeps the sign).
+__device__ __forceinline__ float wrapf(float c, float box) { return fmodf(c, box); }
+
+__device__ __forceinline__ int pick(double u, int n)
+{
+    int k = (int)(u * (double)n);
+    return k < n ? k : n - 1;
+}
+
+__device__ __forceinline__ int discrete(double u, const float *cum, int n)
+{
+    for (int k = 0; k < n - 1; ++k)
+        if (u < (double)cum[k])
+            return k;
+    return n - 1;
+}
+
+// Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with
+// (q*sqrt(DHF), type) in qa/qb.
+__device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float *table, float L,
+                                           float invL)
+{
+    const float dx = min_image(a.x - b.x, L, invL);
+    const float dy = min_image(a.y - b.y, L, invL);
+    const float dz = min_image(a.z - b.z, L, invL);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float inv_r = rsqrt_refined(r2);
+    const float r = r2 * inv_r;
+    const float eij = table[__float_as_int(qa.y) * kTableStride + __float_as_int(qb.y)];
+    const float lj = lj_term(eij, a.w + b.w, inv_r * inv_r);
+    return lj + dh_term(qa.x * qb.x, r, inv_r);
+}
+
+// ------------------------------------------------------------------ move decision
+
+__device__ void decide_move(const EngineArgs &a, const DevSim &S, int g, int r, const uint32_t *w, MoveDesc &mv)
+{
+    const int M = S.M;
+    mv.m = pick(u01(w[0]), M);
+    const DevMol mol = a.mols[S.mol_off + mv.m];
+    mv.start = mol.start;
+    mv.n = mol.count;
+    mv.flexible = (mol.flags & kMolFlexible) != 0;
+    mv.null_move = 0;
+    mv.wrapped = 0;
+    const float box = S.box;
+    const float4 c = __ldcg(&a.center[S.molst_off + (long long)r * M + mv.m]);
+    mv.cx = c.x, mv.cy = c.y, mv.cz = c.z;
+    mv.wcx = c.x, mv.wcy = c.y, mv.wcz = c.z;
+    const double u1 = u01(w[1]);
+    if (mv.flexible)
+        mv.type = (M > 1) ? discrete(u1, S.w_cum, 4) : 1 + discrete(u1, S.w1_cum, 3);
+    else
+        mv.type = (u1 < (double)S.rigid_rotate_p) ? kRotate : kTranslate;  // gsl_ran_bernoulli
+    const double dx = u01(w[2]) - 0.5, dy = 0.5 - u01(w[3]), dz = u01(w[4]) - 0.5;
+    const float tstep = a.tstep[g];
+    const double rstep = a.rstep[g];
+    const long long base = S.state_off + (long long)r * S.N + mv.start;
+
+    switch (mv.type) {
+    case kTranslate: {
+        // Molecule::translate(rng, step) (src/Molecule.cpp:146-159, :262-266)
+        float x = (float)dx, y = (float)dy, z = (float)dz;
+        float mag = sqrtf(x * x + y * y + z * z);
+        if (mag != 0.0f)
+            x /= mag, y /= mag, z /= mag;
+        mv.vx = x * tstep, mv.vy = y * tstep, mv.vz = z * tstep;
+        mv.wcx = wrapf(c.x + mv.vx, box);
+        mv.wcy = wrapf(c.y + mv.vy, box);
+        mv.wcz = wrapf(c.z + mv.vz, box);
+        break;
+    }
+    case kRotate: {
+        // Molecule::rotate(rng, step) -> setRotation (src/Molecule.cpp:193-208, :255-260)
+        double mag = sqrt(dx * dx + dy * dy + dz * dz);
+        axis_angle_matrix(rstep, dx / mag, dy / mag, dz / mag, true, mv.R);
+        break;
+    }
+    case kFlex: {
+        // Molecule::flex(rng, step) (src/Molecule.cpp:331-413)
+        if (mol.nflex == 0) {
+            mv.null_move = 1;
+            break;
+        }
+        double mag = sqrt(dx * dx + dy * dy + dz * dz);
+        axis_angle_matrix(rstep, dx / mag, dy / mag, dz / mag, false, mv.R);
+        const int4 fr = a.flexres[mol.flex_off + pick(u01(w[5]), mol.nflex)];
+        if (fr.y <= 0) {
+            mv.null_move = 1;
+            break;
+        }
+        const int4 op = a.flexopt[fr.z + pick(u01(w[6]), fr.y)];
+        mv.ri = fr.x;
+        mv.br_off = op.y;
+        mv.br_cnt = op.z;
+        const float4 p = __ldcg(&a.pos[base + fr.x]);
+        mv.px = p.x, mv.py = p.y, mv.pz = p.z;
+        break;
+    }
+    case kLocal: {
+        // Molecule::make_local_moves (src/Molecule.cpp:415-448): Bernoulli(0.5) picks a
+        // crankshaft (1) or a local translation (0) of one residue.
+        mv.kind = (u01(w[5]) < 0.5) ? 1 : 0;
+        float vx, vy, vz;
+        if (mv.kind == 0) {
+            if (mol.nlocal == 0) {
+                mv.null_move = 1;
+                break;
+            }
+            mv.ri = a.localres[mol.local_off + pick(u01(w[6]), mol.nlocal)];
+            float x = (float)dx, y = (float)dy, z = (float)dz;
+            float mag = sqrtf(x * x + y * y + z * z);
+            if (mag != 0.0f)
+                x /= mag, y /= mag, z /= mag;
+            const double s = (double)0.1f * (double)tstep;
+            vx = (float)(x * s), vy = (float)(y * s), vz = (float)(z * s);
+        } else {
+            if (mol.ncrank == 0) {
+                mv.null_move = 1;
+                break;
+            }
+            int ri = a.crankres[mol.crank_off + pick(u01(w[6]), mol.ncrank)];
+            if (ri < 1 || ri + 1 >= mv.n) {  // needs both backbone neighbours in the array
+                mv.null_move = 1;
+                break;
+            }
+            mv.ri = ri;
+            const bool flip = u01(w[7]) < 0.5;
+            const float4 pm = __ldcg(&a.pos[base + ri - 1]);
+            const float4 p0 = __ldcg(&a.pos[base + ri]);
+            const float4 pp = __ldcg(&a.pos[base + ri + 1]);
+            double ax = (double)(pp.x - pm.x), ay = (double)(pp.y - pm.y), az = (double)(pp.z - pm.z);
+            double amag = sqrt(ax * ax + ay * ay + az * az);
+            float Rm[9];
+            axis_angle_matrix(flip ? -rstep : rstep, ax / amag, ay / amag, az / amag, true, Rm);
+            const float3 rr = rot_apply(Rm, p0.x - pm.x, p0.y - pm.y, p0.z - pm.z);
+            vx = (rr.x + pm.x) - p0.x;
+            vy = (rr.y + pm.y) - p0.y;
+            vz = (rr.z + pm.z) - p0.z;
+        }
+        // Molecule::translate(v, ri) (src/Molecule.cpp:274-301)
+        const float nf = (float)mv.n;
+        mv.vx = vx, mv.vy = vy, mv.vz = vz;
+        mv.fx = vx / nf, mv.fy = vy / nf, mv.fz = vz / nf;
+        const float ncx = c.x + mv.fx, ncy = c.y + mv.fy, ncz = c.z + mv.fz;
+        const float wx = wrapf(ncx, box), wy = wrapf(ncy, box), wz = wrapf(ncz, box);
+        mv.wrapped = (wx != ncx) || (wy != ncy) || (wz != ncz);
+        mv.wcx = mv.wrapped ? wx : ncx;
+        mv.wcy = mv.wrapped ? wy : ncy;
+        mv.wcz = mv.wrapped ? wz : ncz;
+        break;
+    }
+    }
+    mv.u_metro = u01(w[8]);
+}
+
+// ------------------------------------------------------------------ MC kernel
+
+__global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ MoveDesc mv;
+    __shared__ uint32_t s_w[12];
+    __shared__ double s_red[32];
+    __shared__ double s_old_row, s_pot, s_intrap, s_intra_new;
+    __shared__ int s_accept;
+
+    const int C = a.cluster;
+    const int t = threadIdx.x, T = blockDim.x, lane = t & 31, warp = t >> 5, NW = T >> 5;
+    int rank = 0;
+    if (C > 1)
+        rank = (int)cg::this_cluster().block_rank();
+    const int g = blockIdx.x / C;
+    const int s = a.rep_sim[g];
+    const DevSim S = a.sims[s];
+    const int r = g - S.rep_off;
+    const int N = S.N, M = S.M;
+    const int slice = (a.max_n + C - 1) / C;
+    const SmemLayout Ly = smem_layout(a.max_mol, slice, a.max_m);
+    float *s_table = reinterpret_cast<float *>(smem + Ly.table);
+    float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
+    float4 *s_irel = reinterpret_cast<float4 *>(smem + Ly.irel);
+    int4 *s_iexcl = reinterpret_cast<int4 *>(smem + Ly.iexcl);
+    float4 *s_disp = reinterpret_cast<float4 *>(smem + Ly.idisp);
+    float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
+    float2 *s_ej = reinterpret_cast<float2 *>(smem + Ly.ej);
+    double *s_rowp = reinterpret_cast<double *>(smem + Ly.rowp);
+    double *s_row = reinterpret_cast<double *>(smem + Ly.row);
+
+    for (int k = t; k < kTableStride * kTableStride; k += T)
+        s_table[k] = a.table[k];
+    const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
+    const long long st0 = S.state_off + (long long)r * N;
+    const float4 *stat = a.rstat + S.res_off;
+    const int4 *excl = a.rexcl + S.res_off;
+    double *E = a.emat + S.emat_off + (long long)r * M * M;
+    double *intra = a.intra + S.molst_off + (long long)r * M;
+    float4 *centers = a.center + S.molst_off + (long long)r * M;
+    const uint32_t key0 = a.seed_lo ^ (0x9E3779B9u * (uint32_t)(g + 1)), key1 = a.seed_hi;
+    __syncthreads();
+
+    const unsigned long long step0 = a.stepc[g];
+    for (int step = 0; step < nsteps; ++step) {
+        const unsigned long long mcstep = step0 + (unsigned long long)step;
+        // ---- draws and move decision (thread 0 of every CTA computes the same)
+        if (t < 3) {
+            U4 ctr{(uint32_t)mcstep, (uint32_t)(mcstep >> 32), (uint32_t)t, 0x4D43u};
+            U4 o = philox4x32_10(ctr, key0, key1);
+            s_w[4 * t + 0] = o.x;
+            s_w[4 * t + 1] = o.y;
+            s_w[4 * t + 2] = o.z;
+            s_w[4 * t + 3] = o.w;
+        }
+        __syncthreads();
+        if (t == 0)
+            decide_move(a, S, g, r, s_w, mv);
+        __syncthreads();
+        const int n = mv.n, start = mv.start, type = mv.type;
+        const bool nullm = mv.null_move != 0;
+        const bool flexmol = mv.flexible != 0;
+
+        // ---- old row (read before anyone commits this step)
+        if (warp == 0) {
+            double v = 0.0;
+            for (int b = lane; b < M; b += 32)
+                if (b != mv.m)
+                    v += __ldcg(&E[(long long)mv.m * M + b]);
+            v = warp_sum_d(v);
+            if (lane == 0) {
+                s_old_row = v + __ldcg(&intra[mv.m]);
+                s_pot = __ldcg(&a.potential[g]);
+            }
+        }
+
+        // ---- proposal of the moved molecule
+        for (int i = t; i < n; i += T) {
+            const float4 p = __ldcg(&a.pos[st0 + start + i]);
+            const float4 q = __ldcg(&a.rel[st0 + start + i]);
+            const float4 sr = __ldg(&stat[start + i]);
+            s_iq[i] = make_float2(sr.y, sr.z);
+            if (flexmol)
+                s_iexcl[i] = __ldg(&excl[start + i]);
+            float4 np = p, nq = q;
+            if (!nullm) {
+                if (type == kTranslate) {
+                    np = make_float4(q.x + mv.wcx, q.y + mv.wcy, q.z + mv.wcz, 0.f);
+                } else if (type == kRotate) {
+                    float3 rr = rot_apply(mv.R, q.x, q.y, q.z);
+                    nq = make_float4(rr.x, rr.y, rr.z, 0.f);
+                    np = make_float4(mv.cx + rr.x, mv.cy + rr.y, mv.cz + rr.z, 0.f);
+                } else if (type == kLocal) {
+                    if (i == mv.ri) {
+                        nq = make_float4(q.x + mv.vx, q.y + mv.vy, q.z + mv.vz, 0.f);
+                        np = make_float4(p.x + mv.vx, p.y + mv.vy, p.z + mv.vz, 0.f);
+                    }
+                    nq = make_float4(nq.x - mv.fx, nq.y - mv.fy, nq.z - mv.fz, 0.f);
+                    if (mv.wrapped)
+                        np = make_float4(nq.x + mv.wcx, nq.y + mv.wcy, nq.z + mv.wcz, 0.f);
+                } else {  // kFlex: displacement pass below
+                    s_disp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+            np.w = sr.x;
+            s_ipos[i] = np;
+            s_irel[i] = nq;
+        }
+        __syncthreads();
+        if (type == kFlex && !nullm) {
+            // rotate the branch about the pivot, accumulate the displacement
+            for (int k = t; k < mv.br_cnt; k += T) {
+                const int i = a.branch[mv.br_off + k];
+                const float4 p = s_ipos[i];
+                const float3 rr = rot_apply(mv.R, p.x - mv.px, p.y - mv.py, p.z - mv.pz);
+                s_disp[i] = make_float4((rr.x + mv.px) - p.x, (rr.y + mv.py) - p.y, (rr.z + mv.pz) - p.z, 0.f);
+            }
+            __syncthreads();
+            float sx = 0.f, sy = 0.f, sz = 0.f;
+            for (int i = t; i < n; i += T) {
+                const float4 d = s_disp[i];
+                sx += d.x, sy += d.y, sz += d.z;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sx += __shfl_xor_sync(0xffffffffu, sx, o);
+                sy += __shfl_xor_sync(0xffffffffu, sy, o);
+                sz += __shfl_xor_sync(0xffffffffu, sz, o);
+            }
+            if (lane == 0) {
+                s_red[3 * warp + 0] = sx;  // s_red holds doubles; floats stored exactly
+                s_red[3 * warp + 1] = sy;
+                s_red[3 * warp + 2] = sz;
+            }
+            __syncthreads();
+            if (t == 0) {
+                float ax = 0.f, ay = 0.f, az = 0.f;
+                for (int w = 0; w < NW; ++w)
+                    ax += (float)s_red[3 * w], ay += (float)s_red[3 * w + 1], az += (float)s_red[3 * w + 2];
+                const float nf = (float)n;
+                mv.fx = ax / nf, mv.fy = ay / nf, mv.fz = az / nf;
+                const float ncx = mv.cx + mv.fx, ncy = mv.cy + mv.fy, ncz = mv.cz + mv.fz;
+                const float wx = wrapf(ncx, L), wy = wrapf(ncy, L), wz = wrapf(ncz, L);
+                mv.wrapped = (wx != ncx) || (wy != ncy) || (wz != ncz);
+                mv.wcx = mv.wrapped ? wx : ncx;
+                mv.wcy = mv.wrapped ? wy : ncy;
+                mv.wcz = mv.wrapped ? wz : ncz;
+            }
+            __syncthreads();
+            for (int i = t; i < n; i += T) {
+                const float4 d = s_disp[i];
+                float4 p = s_ipos[i], q = s_irel[i];
+                q = make_float4((q.x + d.x) - mv.fx, (q.y + d.y) - mv.fy, (q.z + d.z) - mv.fz, 0.f);
+                if (mv.wrapped)
+                    p = make_float4(q.x + mv.wcx, q.y + mv.wcy, q.z + mv.wcz, p.w);
+                else
+                    p = make_float4(p.x + d.x, p.y + d.y, p.z + d.z, p.w);
+                s_ipos[i] = p;
+                s_irel[i] = q;
+            }
+            __syncthreads();
+        }
+
+        // ---- inter-molecule pairs: this CTA's slice of the other residues
+        const int nother = N - n;
+        const int o0 = rank * slice, o1 = min(nother, o0 + slice);
+        const int cnt = max(0, o1 - o0);
+        int tpj = 1;
+        if (cnt > 0)
+            while (tpj < 32 && cnt * tpj * 2 <= T)
+                tpj <<= 1;
+        const int sub = t & (tpj - 1), jl = t / tpj, jstride = T / tpj;
+        for (int base = 0; base < cnt; base += jstride) {
+            const int o = o0 + base + jl;
+            const bool valid = (base + jl) < cnt;
+            FF acc{0.f, 0.f};
+            if (valid) {
+                const int j = (o < start) ? o : o + n;
+                const float4 pj = __ldcg(&a.pos[st0 + j]);
+                const float4 sj = __ldg(&stat[j]);
+                const float4 rj = make_float4(pj.x, pj.y, pj.z, sj.x);
+                const float2 qj = make_float2(sj.y, sj.z);
+                float part = 0.f;
+                int cntp = 0;
+                for (int i = sub; i < n; i += tpj) {
+                    part += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                    if (++cntp == 32) {
+                        ff_add(acc, part);
+                        part = 0.f;
+                        cntp = 0;
+                    }
+                }
+                ff_add(acc, part);
+            }
+            for (int o2 = 1; o2 < tpj; o2 <<= 1) {
+                FF w{__shfl_xor_sync(0xffffffffu, acc.hi, o2), __shfl_xor_sync(0xffffffffu, acc.lo, o2)};
+                ff_add_ff(acc, w);
+            }
+            if (valid && sub == 0)
+                s_ej[o - o0] = make_float2(acc.hi, acc.lo);
+        }
+
+        // ---- internal energy of a flexible molecule (intra pairs split over the cluster)
+        FF iacc{0.f, 0.f};
+        if (flexmol) {
+            const int nt = (n + 31) >> 5;
+            const int ntiles = nt * (nt + 1) / 2;
+            for (int k = rank * NW + warp; k < ntiles; k += C * NW) {
+                int ta = 0, rem = k;
+                while (rem >= nt - ta) {
+                    rem -= nt - ta;
+                    ++ta;
+                }
+                const int tb = ta + rem;
+                const int j = tb * 32 + lane;
+                float part = 0.f;
+                if (j < n) {
+                    const float4 pj = s_ipos[j];
+                    const float2 qj = s_iq[j];
+                    const int4 ej = s_iexcl[j];
+                    const int iend = (ta == tb) ? j : min(n, ta * 32 + 32);
+                    for (int i = ta * 32; i < iend; ++i) {
+                        const int4 ei = s_iexcl[i];
+                        const bool ex = (ei.z != 0 && ei.z == ej.z) || (ei.x == ej.x && abs(ei.y - ej.y) < 4) ||
+                                        (ei.w != 0 && ei.w == ej.w);
+                        if (!ex)
+                            part += pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
+                    }
+                }
+                ff_add(iacc, part);
+            }
+            if (rank == 0) {
+                const DevMol mol = a.mols[S.mol_off + mv.m];
+                // indirect neighbours not caught by the rules above
+                for (int k = t; k < mol.nind; k += T) {
+                    const int2 pr = a.indsub[mol.ind_off + k];
+                    ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
+                }
+                // bonds: 0.5 K (r - R0)^2 with the minimum-image distance
+                for (int k = t; k < mol.nbond; k += T) {
+                    const int2 b = a.bonds[mol.bond_off + k];
+                    const float4 pi = s_ipos[b.x], pj = s_ipos[b.y];
+                    const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
+                                dz = min_image(pj.z - pi.z, L, invL);
+                    const float rr = sqrtf(dx * dx + dy * dy + dz * dz) - kR0;
+                    ff_add(iacc, 0.5f * kKSpring * rr * rr);
+                }
+                // angles: -(1/gamma) log(exp(-gamma(ka(t-ta)^2 + ea)) + exp(-gamma kb (t-tb)^2))
+                for (int k = t; k < mol.nang; k += T) {
+                    const int4 an = a.angles[mol.ang_off + k];
+                    const float4 pi = s_ipos[an.x], pj = s_ipos[an.y], pk = s_ipos[an.z];
+                    const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
+                    const float cbx = pk.x - pj.x, cby = pk.y - pj.y, cbz = pk.z - pj.z;
+                    const float cm = sqrtf(cbx * cbx + cby * cby + cbz * cbz) * sqrtf(abx * abx + aby * aby + abz * abz);
+                    float th = 0.f;
+                    if (cm >= 1e-26f)
+                        th = acosf(fminf(1.f, fmaxf(-1.f, (abx * cbx + aby * cby + abz * cbz) / cm)));
+                    const float da = th - kThetaAlpha, db = th - kThetaBeta;
+                    const float term = expf(-kGammaAngle * (kKAlpha * da * da + kEpsAlpha)) +
+                                       expf(-kGammaAngle * (kKBeta * db * db));
+                    ff_add(iacc, -kGammaAngleRecip * logf(term));
+                }
+                // torsions: sum_n V_n (1 + cos(n phi - sigma_n))
+                for (int k = t; k < mol.ntor; k += T) {
+                    const int4 tq = a.tors[mol.tor_off + k];
+                    const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
+                    const float4 p1 = s_ipos[tq.x], p2 = s_ipos[tq.y], p3 = s_ipos[tq.z], p4 = s_ipos[tq.w];
+                    const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
+                    const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
+                    const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
+                    const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
+                    const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
+                    const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
+                    const float phi = atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z),
+                                             c12x * c23x + c12y * c23y + c12z * c23z);
+                    const float e = V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
+                                    V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
+                    ff_add(iacc, e);
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- per-molecule partial rows of this CTA's slice
+        for (int b = warp; b < M; b += NW) {
+            FF acc{0.f, 0.f};
+            if (b != mv.m) {
+                const DevMol mb = a.mols[S.mol_off + b];
+                const int ob0 = (mb.start < start) ? mb.start : mb.start - n;
+                const int lo = max(ob0, o0), hi = min(ob0 + mb.count, o1);
+                for (int o = lo + lane; o < hi; o += 32) {
+                    const float2 e = s_ej[o - o0];
+                    ff_add_ff(acc, FF{e.x, e.y});
+                }
+                acc = ff_warp_sum(acc);
+            }
+            if (lane == 0)
+                s_rowp[b] = (b != mv.m) ? ff_value(acc) : 0.0;
+        }
+        {
+            const double v = block_sum_d(ff_value(iacc), s_red);
+            if (t == 0)
+                s_intrap = v;
+        }
+        if (C > 1)
+            cg::this_cluster().sync();
+        else
+            __syncthreads();
+
+        // ---- gather the cluster's partials (fixed rank order), Metropolis
+        if (C > 1) {
+            cg::cluster_group cl = cg::this_cluster();
+            for (int b = t; b < M; b += T) {
+                double v = 0.0;
+                for (int k = 0; k < C; ++k)
+                    v += cl.map_shared_rank(s_rowp, k)[b];
+                s_row[b] = v;
+            }
+            if (t == 0) {
+                double v = 0.0;
+                for (int k = 0; k < C; ++k)
+                    v += *cl.map_shared_rank(&s_intrap, k);
+                s_intra_new = v;
+            }
+        } else {
+            for (int b = t; b < M; b += T)
+                s_row[b] = s_rowp[b];
+            if (t == 0)
+                s_intra_new = s_intrap;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double v = 0.0;
+            for (int b = lane; b < M; b += 32)
+                if (b != mv.m)
+                    v += s_row[b];
+            v = warp_sum_d(v);
+            if (lane == 0) {
+                const double new_row = v + (flexmol ? s_intra_new : 0.0);
+                const double newPotential = s_pot - s_old_row + new_row;
+                const float delta = (float)(newPotential - s_pot);
+                int acc = 0;
+                if (delta < 0.0f) {
+                    acc = 1;
+                } else {
+                    const float T_ = a.temperature[g];
+                    const float boltz = expf(-(delta * kKcal) / (kRgas * T_));
+                    acc = (mv.u_metro < (double)boltz) ? 2 : 0;
+                }
+                if (!isfinite(newPotential))
+                    acc = 0;
+                s_accept = acc;
+                s_pot = acc ? newPotential : s_pot;
+            }
+        }
+        __syncthreads();
+
+        // ---- commit (rank 0 only)
+        if (rank == 0) {
+            const int acc = s_accept;
+            if (acc) {
+                for (int i = t; i < n; i += T) {
+                    float4 p = s_ipos[i];
+                    p.w = 0.f;
+                    a.pos[st0 + start + i] = p;
+                    a.rel[st0 + start + i] = s_irel[i];
+                }
+                for (int b = t; b < M; b += T)
+                    if (b != mv.m) {
+                        E[(long long)mv.m * M + b] = s_row[b];
+                        E[(long long)b * M + mv.m] = s_row[b];
+                    }
+                if (t == 0) {
+                    centers[mv.m] = make_float4(mv.wcx, mv.wcy, mv.wcz, 0.f);
+                    if (flexmol)
+                        intra[mv.m] = s_intra_new;
+                    a.potential[g] = s_pot;
+                }
+            }
+            if (t == 0) {
+                const DevMol mm = a.mols[S.mol_off + mv.m];
+                a.pairc[g] += (unsigned long long)n * (unsigned long long)(N - n) +
+                              (flexmol ? (unsigned long long)mm.nintra : 0ull);
+                ReplicaStats &stt = a.stats[g];
+                if (acc == 1)
+                    stt.accept++;
+                else if (acc == 2)
+                    stt.acceptA++;
+                else
+                    stt.reject++;
+                if (mv.null_move)
+                    atomicOr(&a.errflags[g], 1u);
+            }
+            // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
+            const int freq = S.sample_freq;
+            if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&
+                (long long)mcstep >= (long long)S.sample_after) {
+                __syncthreads();
+                if (warp == 0) {
+                    double e = 0.0;
+                    if (S.nc_mode == 1) {
+                        const int nc = S.non_crowders;
+                        for (int k = lane; k < nc * nc; k += 32) {
+                            const int aa = k / nc, bb = k % nc;
+                            if (aa < bb)
+                                e += E[(long long)aa * M + bb];
+                        }
+                        e = warp_sum_d(e);
+                    } else if (S.nc_mode == 2) {
+                        e = s_pot;
+                    }
+                    if (lane == 0) {
+                        ReplicaStats &stt = a.stats[g];
+                        stt.samplesSinceLastExchange++;
+                        if ((float)e < S.bound_threshold)
+                            stt.boundSamples++;
+                    }
+                }
+            }
+        }
+        if (C > 1)
+            cg::this_cluster().sync();
+        else
+            __syncthreads();
+    }
+    if (rank == 0 && t == 0)
+        a.stepc[g] += (unsigned long long)nsteps;
+}
+
+// ------------------------------------------------------------------ initial energies
+
+// CTA (g, a): row a of replica g's matrix for b > a, and the internal energy of a.
+__global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32];
+    const int t = threadIdx.x, T = blockDim.x, lane = t & 31, warp = t >> 5, NW = T >> 5;
+    const int g = blockIdx.x / a.max_m, am = blockIdx.x % a.max_m;
+    const int s = a.rep_sim[g];
+    const DevSim S = a.sims[s];
+    if (am >= S.M)
+        return;
+    const int r = g - S.rep_off, N = S.N, M = S.M;
+    const SmemLayout Ly = smem_layout(a.max_mol, a.max_n, a.max_m);
+    float *s_table = reinterpret_cast<float *>(smem + Ly.table);
+    float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
+    float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
+    int4 *s_iexcl = reinterpret_cast<int4 *>(smem + Ly.iexcl);
+    for (int k = t; k < kTableStride * kTableStride; k += T)
+        s_table[k] = a.table[k];
+    const DevMol mol = a.mols[S.mol_off + am];
+    const long long st0 = S.state_off + (long long)r * N;
+    const float4 *stat = a.rstat + S.res_off;
+    const int4 *excl = a.rexcl + S.res_off;
+    const int n = mol.count, start = mol.start;
+    for (int i = t; i < n; i += T) {
+        const float4 p = a.pos[st0 + start + i];
+        const float4 sr = stat[start + i];
+        s_ipos[i] = make_float4(p.x, p.y, p.z, sr.x);
+        s_iq[i] = make_float2(sr.y, sr.z);
+        s_iexcl[i] = excl[start + i];
+    }
+    __syncthreads();
+    const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
+    double *E = a.emat + S.emat_off + (long long)r * M * M;
+    for (int b = am + 1; b < M; ++b) {
+        const DevMol mb = a.mols[S.mol_off + b];
+        FF acc{0.f, 0.f};
+        for (int jj = t; jj < mb.count; jj += T) {
+            const int j = mb.start + jj;
+            const float4 pj = a.pos[st0 + j];
+            const float4 sj = stat[j];
+            const float4 rj = make_float4(pj.x, pj.y, pj.z, sj.x);
+            const float2 qj = make_float2(sj.y, sj.z);
+            float part = 0.f;
+            for (int i = 0; i < n; ++i) {
+                part += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                if ((i & 31) == 31) {
+                    ff_add(acc, part);
+                    part = 0.f;
+                }
+            }
+            ff_add(acc, part);
+        }
+        const double v = block_sum_d(ff_value(acc), s_red);
+        if (t == 0) {
+            E[(long long)am * M + b] = v;
+            E[(long long)b * M + am] = v;
+        }
+    }
+    if (t == 0)
+        E[(long long)am * M + am] = 0.0;
+    FF iacc{0.f, 0.f};
+    if (mol.flags & kMolFlexible) {
+        for (int j = t; j < n; j += T) {
+            const float4 pj = s_ipos[j];
+            const float2 qj = s_iq[j];
+            const int4 ej = s_iexcl[j];
+            float part = 0.f;
+            for (int i = 0; i < j; ++i) {
+                const int4 ei = s_iexcl[i];
+                const bool ex = (ei.z != 0 && ei.z == ej.z) || (ei.x == ej.x && abs(ei.y - ej.y) < 4) ||
+                                (ei.w != 0 && ei.w == ej.w);
+                if (!ex)
+                    part += pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
+                if ((i & 31) == 31) {
+                    ff_add(iacc, part);
+                    part = 0.f;
+                }
+            }
+            ff_add(iacc, part);
+        }
+        for (int k = t; k < mol.nind; k += T) {
+            const int2 pr = a.indsub[mol.ind_off + k];
+            ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
+        }
+        for (int k = t; k < mol.nbond; k += T) {
+            const int2 b = a.bonds[mol.bond_off + k];
+            const float4 pi = s_ipos[b.x], pj = s_ipos[b.y];
+            const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
+                        dz = min_image(pj.z - pi.z, L, invL);
+            const float rr = sqrtf(dx * dx + dy * dy + dz * dz) - kR0;
+            ff_add(iacc, 0.5f * kKSpring * rr * rr);
+        }
+        for (int k = t; k < mol.nang; k += T) {
+            const int4 an = a.angles[mol.ang_off + k];
+            const float4 pi = s_ipos[an.x], pj = s_ipos[an.y], pk = s_ipos[an.z];
+            const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
+            const float cbx = pk.x - pj.x, cby = pk.y - pj.y, cbz = pk.z - pj.z;
+            const float cm = sqrtf(cbx * cbx + cby * cby + cbz * cbz) * sqrtf(abx * abx + aby * aby + abz * abz);
+            float th = 0.f;
+            if (cm >= 1e-26f)
+                th = acosf(fminf(1.f, fmaxf(-1.f, (abx * cbx + aby * cby + abz * cbz) / cm)));
+            const float da = th - kThetaAlpha, db = th - kThetaBeta;
+            const float term =
+                expf(-kGammaAngle * (kKAlpha * da * da + kEpsAlpha)) + expf(-kGammaAngle * (kKBeta * db * db));
+            ff_add(iacc, -kGammaAngleRecip * logf(term));
+        }
+        for (int k = t; k < mol.ntor; k += T) {
+            const int4 tq = a.tors[mol.tor_off + k];
+            const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
+            const float4 p1 = s_ipos[tq.x], p2 = s_ipos[tq.y], p3 = s_ipos[tq.z], p4 = s_ipos[tq.w];
+            const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
+            const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
+            const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
+            const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
+            const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
+            const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
+            const float phi =
+                atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), c12x * c23x + c12y * c23y + c12z * c23z);
+            const float e = V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
+                            V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
+            ff_add(iacc, e);
+        }
+    }
+    const double v = block_sum_d(ff_value(iacc), s_red);
+    if (t == 0)
+        a.intra[S.molst_off + (long long)r * M + am] = (mol.flags & kMolFlexible) ? v : 0.0;
+    (void)lane, (void)warp, (void)NW;
+}
+
+// potential[g] = sum_{a<b} E[a][b] + sum_a intra[a]
+__global__ void k_sum_potential(EngineArgs a, double *out)
+{
+    const int g = blockIdx.x, lane = threadIdx.x;
+    const DevSim S = a.sims[a.rep_sim[g]];
+    const int r = g - S.rep_off, M = S.M;
+    const double *E = a.emat + S.emat_off + (long long)r * M * M;
+    const double *in = a.intra + S.molst_off + (long long)r * M;
+    double v = 0.0;
+    for (int k = lane; k < M * M; k += 32) {
+        const int x = k / M, y = k % M;
+        if (x < y)
+            v += E[k];
+    }
+    for (int k = lane; k < M; k += 32)
+        v += in[k];
+    v = warp_sum_d(v);
+    if (lane == 0)
+        out[g] = v;
+}
+
+// ------------------------------------------------------------------ exchange
+
+__device__ void report_slot(ReplicaStats &s, float4 &out)
+{
+    // Replica::fraction_bound and Replica::acceptance_ratio (src/Replica.cpp:1095-1122)
+    s.totalBoundSamples += s.boundSamples;
+    s.totalSamples += s.samplesSinceLastExchange;
+    s.fractionBound = (float)s.boundSamples / fmaxf(1.0f, (float)s.samplesSinceLastExchange);
+    s.accumulativeFractionBound = (float)s.totalBoundSamples / fmaxf(1.0f, (float)s.totalSamples);
+    s.boundSamples = 0;
+    s.samplesSinceLastExchange = 0;
+    s.totalAccept += s.acceptA + s.accept;
+    s.totalAcceptReject += s.acceptA + s.accept + s.reject;
+    s.acceptanceRatio = (float)(s.acceptA + s.accept) / (float)(s.acceptA + s.accept + s.reject);
+    s.accumulativeAcceptanceRatio = (float)s.totalAccept / (float)s.totalAcceptReject;
+    s.acceptA = s.accept = s.reject = 0;
+    out = make_float4(s.fractionBound, s.accumulativeFractionBound, s.acceptanceRatio, s.accumulativeAcceptanceRatio);
+}
+
+// One warp per simulation.  mode bit 0: write the per-temperature report first; bit 1:
+// perform the exchange sweep.  `report_row` selects the report slot.
+__global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block)
+{
+    const int s = blockIdx.x;
+    if (threadIdx.x != 0)
+        return;
+    const DevSim S = a.sims[s];
+    int *st = a.sim_state + 4 * s;
+    const int x = st[1];
+    const int R = S.R;
+    // reporting happens when sampling has started (src/Simulation.cpp:751-768)
+    if ((long long)steps_per_block * x >= (long long)S.sample_after && x < a.report_capacity) {
+        for (int tt = 0; tt < R; ++tt) {
+            const int slot = a.slot_of_t[S.rep_off + tt];
+            float4 o;
+            report_slot(a.stats[S.rep_off + slot], o);
+            a.report[(long long)x * total_replicas + S.rep_off + tt] = o;
+        }
+    }
+    int exchanges = 0, tests = 0;
+    const int offset = st[0];
+    for (int ti = offset; ti < R - 1; ti += 2) {
+        const int i = a.slot_of_t[S.rep_off + ti], j = a.slot_of_t[S.rep_off + ti + 1];
+        const int gi = S.rep_off + i, gj = S.rep_off + j;
+        const double Ti = a.temperature[gi], Tj = a.temperature[gj];
+        const double delta =
+            (1.0 / Ti - 1.0 / Tj) * (a.potential[gi] - a.potential[gj]) * (double)(kKcal / kRgas);
+        U4 ctr{(uint32_t)x, 0u, (uint32_t)ti, 0x5245u};
+        const U4 o = philox4x32_10(ctr, a.seed_lo ^ 0xB5297A4Du, a.seed_hi ^ (0x68E31DA4u * (uint32_t)(s + 1)));
+        if (u01(o.x) < fmin(1.0, exp(delta))) {
+            // Replica::exchangeReplicas: swap temperature, label and statistics
+            float tf = a.temperature[gi];
+            a.temperature[gi] = a.temperature[gj];
+            a.temperature[gj] = tf;
+            int ti_ = a.tindex[gi];
+            a.tindex[gi] = a.tindex[gj];
+            a.tindex[gj] = ti_;
+            int lb = a.label[gi];
+            a.label[gi] = a.label[gj];
+            a.label[gj] = lb;
+            ReplicaStats sv = a.stats[gi];
+            a.stats[gi] = a.stats[gj];
+            a.stats[gj] = sv;
+            a.slot_of_t[S.rep_off + a.tindex[gi]] = i;
+            a.slot_of_t[S.rep_off + a.tindex[gj]] = j;
+            ++exchanges;
+        }
+        ++tests;
+    }
+    st[0] = 1 - offset;
+    if (x < a.report_capacity)
+        a.exch_report[(long long)x * gridDim.x + s] = make_int2(exchanges, tests);
+    st[2] += exchanges;
+    st[3] += tests;
+    st[1] = x + 1;
+}
+
+// Final per-temperature report after the last block (src/Simulation.cpp:834-848).
+__global__ void k_final_report(EngineArgs a, int total_replicas, int row)
+{
+    const int s = blockIdx.x;
+    if (threadIdx.x != 0)
+        return;
+    const DevSim S = a.sims[s];
+    for (int tt = 0; tt < S.R; ++tt) {
+        const int slot = a.slot_of_t[S.rep_off + tt];
+        float4 o;
+        report_slot(a.stats[S.rep_off + slot], o);
+        if (row < a.report_capacity)
+            a.report[(long long)row * total_replicas + S.rep_off + tt] = o;
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+
+cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
+                            cudaStream_t stream)
+{
+    const int C = a.cluster;
+    if (C > 1) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(total_replicas * C);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_mc_block, a, nsteps);
+    }
+    k_mc_block<<<total_replicas, threads, smem, stream>>>(a, nsteps);
+    return cudaGetLastError();
+}
+
+cudaError_t set_mc_smem_limit(size_t smem)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_mc_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    e = cudaFuncSetAttribute(k_init_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_mc_block, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
+cudaError_t launch_init_energy(const EngineArgs &a, int total_replicas, size_t smem, double *potential_out,
+                               cudaStream_t stream)
+{
+    k_init_rows<<<total_replicas * a.max_m, 256, smem, stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    k_sum_potential<<<total_replicas, 32, 0, stream>>>(a, potential_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exchange(const EngineArgs &a, int nsims, int total_replicas, int steps_per_block,
+                            cudaStream_t stream)
+{
+    k_exchange<<<nsims, 32, 0, stream>>>(a, total_replicas, steps_per_block);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_final_report(const EngineArgs &a, int nsims, int total_replicas, int row, cudaStream_t stream)
+{
+    k_final_report<<<nsims, 32, 0, stream>>>(a, total_replicas, row);
+    return cudaGetLastError();
+}
+
+}  // namespace cgppd

@@ -1,0 +1,116 @@
+// engine_types.h -- device data layout of the batched replica-exchange engine.
+//
+// One engine holds S independent simulations.  Simulation s has N residues in M
+// molecules (contiguous, argfile order) and R replicas; all replicas of all
+// simulations are advanced by one kernel launch (one CTA cluster per replica).
+//
+// HBM layout (all arrays flat, offsets in DevSim):
+//   static, per residue   rstat[res_off+i]  float4 (sigma_i/2, q_i*sqrt(DHF), type bits, mol bits)
+//                          rexcl[res_off+i]  int4   (chain uid, resSeq, domain uid, bond uid)
+//   static, per molecule  mols[mol_off+m]   DevMol (range, flags, graph list offsets)
+//   per replica state     pos/rel[state_off + r*N + i]  float4 (x, y, z, 0)
+//                          center[molst_off + r*M + m]   float4
+//                          emat[emat_off + r*M*M + a*M + b]  double, pair energy of molecules a, b
+//                          intra[molst_off + r*M + m]   double, intra + bonded energy of molecule m
+//                          potential/temperature/steps/stats[rep_off + r]
+#pragma once
+
+#include <cstdint>
+#include <vector_types.h>
+
+namespace cgppd {
+
+enum MoveType { kTranslate = 0, kRotate = 1, kFlex = 2, kLocal = 3 };
+enum MolFlags { kMolFlexible = 1, kMolCrowder = 2 };
+
+struct DevSim {
+    int N, M, R;
+    int res_off;                 // first static residue
+    int mol_off;                 // first static molecule
+    int rep_off;                 // first global replica
+    long long state_off;         // residue state of replica 0 (replicas stride N)
+    int molst_off;               // molecule state of replica 0 (replicas stride M)
+    long long emat_off;          // energy matrix of replica 0 (replicas stride M*M)
+    float box, inv_box;
+    float w_cum[4];              // cumulative move weights of a flexible molecule (T, R, F, L)
+    float w1_cum[3];             // same when it is the only molecule (R, F, L)
+    float rigid_rotate_p;        // P(rotate) for a rigid molecule (Bernoulli, else translate)
+    int non_crowders;            // molecules before the first crowder
+    int nc_mode;                 // 0: bound test uses 0; 1: non-crowder inter energy; 2: potential
+    int sample_freq, sample_after;
+    float bound_threshold;       // kcal/mol, BOUND_ENERGY_VALUE
+    int max_mol;                 // largest molecule
+    int pad0;
+};
+
+struct DevMol {
+    int start, count, flags;
+    int bond_off, nbond;
+    int ang_off, nang;
+    int tor_off, ntor;
+    int ind_off, nind;           // indirect-neighbour pairs to subtract (not otherwise excluded)
+    int flex_off, nflex;         // flexible residues: int4 (ri, degree, option offset, 0)
+    int local_off, nlocal;
+    int crank_off, ncrank;
+    int nintra;                  // intra pairs that are not excluded (flexible molecules)
+};
+
+// Per-replica counters and ratios, swapped with the temperature on exchange
+// (src/Replica.cpp:188-210).
+struct ReplicaStats {
+    int accept, acceptA, reject;
+    int totalAcceptReject, totalAccept;
+    int boundSamples, samplesSinceLastExchange;
+    int totalBoundSamples, totalSamples;
+    float acceptanceRatio, accumulativeAcceptanceRatio;
+    float fractionBound, accumulativeFractionBound;
+    int pad[3];
+};
+
+struct EngineArgs {
+    const DevSim *sims;
+    const int *rep_sim;          // global replica -> simulation
+    const DevMol *mols;
+    const float4 *rstat;
+    const int4 *rexcl;
+    const int2 *bonds;
+    const int4 *angles;          // (i, j, k, 0)
+    const int4 *tors;            // (i, j, k, l)
+    const float4 *torsV;         // amplitudes V1..V4 of each torsion
+    const float4 *torsS;         // phases (rad) of each torsion
+    const int2 *indsub;
+    const int4 *flexres;         // (ri, degree, first option, 0)
+    const int4 *flexopt;         // (neighbour, branch offset, branch count, 0)
+    const int *branch;
+    const int *localres;
+    const int *crankres;
+    const float *table;          // Eij in kcal/mol, ntypes x ntypes (row stride 32)
+    float4 *pos;
+    float4 *rel;
+    float4 *center;
+    double *emat;
+    double *intra;
+    double *potential;
+    float *temperature;
+    float *tstep;
+    double *rstep;
+    unsigned long long *stepc;   // MC steps done by each replica
+    unsigned long long *pairc;   // residue-pair terms evaluated by each replica
+    ReplicaStats *stats;
+    int *tindex;                 // temperature-ladder index held by each replica slot
+    int *label;
+    int *slot_of_t;              // [rep_off + t] replica slot holding ladder index t
+    int *sim_state;              // per simulation: {offset, exchanges done, exch_total, tests_total}
+    float4 *report;              // per exchange and ladder index: (fb, afb, ar, aar)
+    int2 *exch_report;           // per exchange: (exchanges, tests)
+    int report_capacity;         // exchanges the report buffers hold per simulation
+    unsigned *errflags;          // per replica error bits
+    uint32_t seed_lo, seed_hi;
+    int ntypes;
+    int cluster;                 // CTAs per replica
+    int max_n;                   // largest N
+    int max_m;                   // largest M
+    int max_mol;                 // largest molecule
+};
+
+}  // namespace cgppd

@@ -37,6 +37,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "cgppd_oracle_internal.h"
+
 #define ORACLE_REF 0
 #define ORACLE_FP64 1
 
@@ -91,7 +93,7 @@ static double dist_fp64(const float *a, const float *b, float L)
     return sqrt(X * X + Y * Y + Z * Z);
 }
 
-static double dist(int mode, const float *a, const float *b, float L)
+double or_dist(int mode, const float *a, const float *b, float L)
 {
     return mode == ORACLE_REF ? dist_ref(a, b, L) : dist_fp64(a, b, L);
 }
@@ -100,7 +102,7 @@ static double dist(int mode, const float *a, const float *b, float L)
 
 /* calculate_LJ (src/Potential.cpp:5-35).  eps_raw is the table value
  * LJpotentials[a][b] (float, RT units, before the lambda/e0 transform). */
-static double lj_term(int mode, double r, float eps_raw, float si, float sj)
+double or_lj_term(int mode, double r, float eps_raw, float si, float sj)
 {
     if (mode == ORACLE_REF) {
         double Eij = (double)(OR_LAMBDA * (eps_raw - OR_E0));
@@ -122,7 +124,7 @@ static double lj_term(int mode, double r, float eps_raw, float si, float sj)
 }
 
 /* calculate_DH (src/Potential.cpp:37-42): q_i q_j expf(-r/xi) / r. */
-static double dh_term(int mode, double r, float qi, float qj)
+double or_dh_term(int mode, double r, float qi, float qj)
 {
     if (mode == ORACLE_REF)
         return (double)(qi * qj * expf((float)(-r / OR_XI))) / r;
@@ -133,9 +135,9 @@ static double dh_term(int mode, double r, float qi, float qj)
 void oracle_pair(int mode, const float *pi, const float *pj, float eps_raw, float qi,
                  float qj, float si, float sj, float box, double *lj, double *dh)
 {
-    double r = dist(mode, pi, pj, box) + (double)OR_EPS;
-    *lj = lj_term(mode, r, eps_raw, si, sj);
-    *dh = dh_term(mode, r, qi, qj);
+    double r = or_dist(mode, pi, pj, box) + (double)OR_EPS;
+    *lj = or_lj_term(mode, r, eps_raw, si, sj);
+    *dh = or_dh_term(mode, r, qi, qj);
 }
 
 /* ---------------------------------------------------------------- sums */
@@ -153,9 +155,9 @@ void oracle_E_inter(int mode, int nmol, const int *mstart, const int *mcount,
         for (int mJ = mI + 1; mJ < nmol; mJ++)
             for (int a = mstart[mI]; a < mstart[mI] + mcount[mI]; a++)
                 for (int b = mstart[mJ]; b < mstart[mJ] + mcount[mJ]; b++) {
-                    double r = dist(mode, xyz + 3 * a, xyz + 3 * b, box) + (double)OR_EPS;
-                    LJ += lj_term(mode, r, table[aa[a] * ntypes + aa[b]], sig[a], sig[b]);
-                    DH += dh_term(mode, r, q[a], q[b]);
+                    double r = or_dist(mode, xyz + 3 * a, xyz + 3 * b, box) + (double)OR_EPS;
+                    LJ += or_lj_term(mode, r, table[aa[a] * ntypes + aa[b]], sig[a], sig[b]);
+                    DH += or_dh_term(mode, r, q[a], q[b]);
                 }
     *out_lj = LJ;
     *out_dh = DH;
@@ -173,9 +175,9 @@ void oracle_E_inter_matrix(int mode, int nmol, const int *mstart, const int *mco
             double LJ = 0.0, DH = 0.0;
             for (int a = mstart[mI]; a < mstart[mI] + mcount[mI]; a++)
                 for (int b = mstart[mJ]; b < mstart[mJ] + mcount[mJ]; b++) {
-                    double r = dist(mode, xyz + 3 * a, xyz + 3 * b, box) + (double)OR_EPS;
-                    LJ += lj_term(mode, r, table[aa[a] * ntypes + aa[b]], sig[a], sig[b]);
-                    DH += dh_term(mode, r, q[a], q[b]);
+                    double r = or_dist(mode, xyz + 3 * a, xyz + 3 * b, box) + (double)OR_EPS;
+                    LJ += or_lj_term(mode, r, table[aa[a] * ntypes + aa[b]], sig[a], sig[b]);
+                    DH += or_dh_term(mode, r, q[a], q[b]);
                 }
             double e = LJ * OR_RT_TO_KCAL + DH * OR_DHC;
             out[mI * nmol + mJ] = e;
@@ -185,7 +187,7 @@ void oracle_E_inter_matrix(int mode, int nmol, const int *mstart, const int *mco
 
 /* Vector3f::angle (src/vector3f.cpp:137-143) as the reference computes it: float
  * magnitudes and dot product, double acos, float result. */
-static double angle_ref(const float *a, const float *b)
+double or_angle_ref(const float *a, const float *b)
 {
     float ma = sqrtf(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
     float mb = sqrtf(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
@@ -196,7 +198,7 @@ static double angle_ref(const float *a, const float *b)
     return (double)(float)acos(dot / cmag);
 }
 
-static double angle_fp64(const float *pa, const float *pb, const float *pc)
+double or_angle_fp64(const float *pa, const float *pb, const float *pc)
 {
     double a[3], b[3];
     for (int k = 0; k < 3; k++) {
@@ -213,7 +215,7 @@ static double angle_fp64(const float *pa, const float *pb, const float *pc)
 }
 
 /* calculate_angle (src/Potential.cpp:57-71): the term whose product is stored. */
-static double angle_term(double theta)
+double or_angle_term(double theta)
 {
     double da = theta - (double)OR_THETA_ALPHA, db = theta - (double)OR_THETA_BETA;
     return exp(-(double)OR_GAMMA * ((double)OR_K_ALPHA * da * da + (double)OR_EPS_ALPHA)) +
@@ -235,7 +237,7 @@ static void cross3f(const float *a, const float *b, float *o)
 }
 
 /* The dihedral of calculate_torsion (src/Potential.cpp:73-98). */
-static double torsion_phi(int mode, const float *pi, const float *pj, const float *pk, const float *pl)
+double or_torsion_phi(int mode, const float *pi, const float *pj, const float *pk, const float *pl)
 {
     if (mode == ORACLE_REF) {
         float b1[3], b2[3], b3[3], c23[3], c12[3];
@@ -298,21 +300,21 @@ void oracle_E_intra(int mode, int n, const float *xyz, const int *aa, const floa
                     }
                 if (same_domain || chain_nb || bonded || ind)
                     continue;
-                double r = dist(mode, xyz + 3 * i, xyz + 3 * j, box) + (double)OR_EPS;
-                LJ += lj_term(mode, r, table[aa[i] * ntypes + aa[j]], sig[i], sig[j]);
-                DH += dh_term(mode, r, q[i], q[j]);
+                double r = or_dist(mode, xyz + 3 * i, xyz + 3 * j, box) + (double)OR_EPS;
+                LJ += or_lj_term(mode, r, table[aa[i] * ntypes + aa[j]], sig[i], sig[j]);
+                DH += or_dh_term(mode, r, q[i], q[j]);
             }
     } else {
         for (int p = 0; p < n_ind; p++) {
             int i = indirect[2 * p], j = indirect[2 * p + 1];
-            double r = dist(mode, xyz + 3 * i, xyz + 3 * j, box) + (double)OR_EPS;
-            LJ -= lj_term(mode, r, table[aa[i] * ntypes + aa[j]], sig[i], sig[j]);
-            DH -= dh_term(mode, r, q[i], q[j]);
+            double r = or_dist(mode, xyz + 3 * i, xyz + 3 * j, box) + (double)OR_EPS;
+            LJ -= or_lj_term(mode, r, table[aa[i] * ntypes + aa[j]], sig[i], sig[j]);
+            DH -= or_dh_term(mode, r, q[i], q[j]);
         }
     }
     for (int b = 0; b < n_bonds; b++) {
         int i = bonds[2 * b], j = bonds[2 * b + 1];
-        double r = dist(mode, xyz + 3 * j, xyz + 3 * i, box);
+        double r = or_dist(mode, xyz + 3 * j, xyz + 3 * i, box);
         double d = r - (double)OR_R0;
         B += d * d;
     }
@@ -324,15 +326,15 @@ void oracle_E_intra(int mode, int n, const float *xyz, const int *aa, const floa
             float ab[3], cb[3];
             sub3f(pi, pj, ab);
             sub3f(pk, pj, cb);
-            theta = angle_ref(ab, cb);
+            theta = or_angle_ref(ab, cb);
         } else {
-            theta = angle_fp64(pi, pj, pk);
+            theta = or_angle_fp64(pi, pj, pk);
         }
-        A *= angle_term(theta);
+        A *= or_angle_term(theta);
     }
     for (int t = 0; t < n_tors; t++) {
         const int *tt = tors + 4 * t;
-        double phi = torsion_phi(mode, xyz + 3 * tt[0], xyz + 3 * tt[1], xyz + 3 * tt[2], xyz + 3 * tt[3]);
+        double phi = or_torsion_phi(mode, xyz + 3 * tt[0], xyz + 3 * tt[1], xyz + 3 * tt[2], xyz + 3 * tt[3]);
         int r1 = aa[tt[1]], r2 = aa[tt[2]];
         const double *V = torsV + 4 * (r1 * ntypes_t + r2), *S = torsS + 4 * (r1 * ntypes_t + r2);
         double pot = 0.0;
@@ -401,10 +403,10 @@ void oracle_E_packed(int mode, int nc, int P, const float *pos4, const float *me
             }
             if (excluded)
                 continue;
-            double r = dist(mode, px, py, box) + (double)OR_EPS;
+            double r = or_dist(mode, px, py, box) + (double)OR_EPS;
             int ax = (int)rintf(mx[0]), ay = (int)rintf(my[0]);
-            LJ += lj_term(mode, r, table20[ay * 20 + ax], my[2], mx[2]);
-            DH += dh_term(mode, r, my[1], mx[1]);
+            LJ += or_lj_term(mode, r, table20[ay * 20 + ax], my[2], mx[2]);
+            DH += or_dh_term(mode, r, my[1], mx[1]);
         }
     }
     out[0] = LJ;

@@ -1,0 +1,203 @@
+"""Parity of the batched GB300 REMC engine with the oracle.
+
+1. Energies: every replica's molecule-pair matrix, internal energies and total are
+   compared with the FP64 oracle on the same coordinates (1e-5 relative bound).
+2. Trajectories: the engine and the oracle's restatement of the reference MC loop
+   (full recomputation each step, reference precision) draw the same Philox words, so
+   they take the same moves and -- except for Metropolis draws that fall within float
+   rounding of the acceptance probability -- the same decisions.  Positions are compared
+   after whole blocks (tolerance 2e-3 A for the accumulated float rotations), potentials
+   within 1e-5 relative, exchange decisions and counters exactly.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cgppd_gb300 import engine as eng
+from cgppd_gb300 import workloads
+from oracle.remc import OracleRemc, float_mean
+
+pytestmark = pytest.mark.gpu
+REL = 1e-5
+
+
+def oracle_matrix(wl, sim, xyz):
+    mols = sim.molecules
+    start = np.cumsum([0] + [m.n for m in mols[:-1]]).astype(np.int32)
+    cnt = np.array([m.n for m in mols], np.int32)
+    aa = np.concatenate([m.types for m in mols])
+    q = np.concatenate([m.charges for m in mols])
+    s = np.concatenate([m.radii for m in mols])
+    return oracle.E_inter_matrix(oracle.FP64, xyz, aa, q, s, start, cnt, wl.lj_raw, sim.box)
+
+
+def subset(wl, nrep):
+    sim = wl.sims[0]
+    return workloads.Simulation(sim.molecules, sim.box, sim.temperatures[:nrep], sim.translate_steps[:nrep],
+                                sim.rotate_steps[:nrep], sim.move_weights, sim.rigid_rotate_prob)
+
+
+def engine_for(wl, sims, cluster=1, threads=256, sample_frequency=0, sample_after=0):
+    w2 = workloads.Workload(wl.name, sims, wl.lj_raw, wl.torsion_V, wl.torsion_phase, wl.seed)
+    return eng.from_workload(w2, cluster=cluster, threads=threads, sample_frequency=sample_frequency,
+                             sample_after=sample_after)
+
+
+def oracle_for(wl, sim, mode=oracle.REF, **kw):
+    return OracleRemc(sim.molecules, wl.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
+                      sim.move_weights, sim.rigid_rotate_prob, wl.torsion_V, wl.torsion_phase, seed=wl.seed,
+                      mode=mode, **kw)
+
+
+@pytest.mark.parametrize("config", ["c0", "c2", "c4"])
+def test_initial_energy_matrix(config):
+    wl = workloads.make(config)
+    sim = subset(wl, 2)
+    e = engine_for(wl, [sim])
+    xyz = np.concatenate([m.xyz for m in sim.molecules]).astype(np.float32)
+    ref = oracle_matrix(wl, sim, xyz)
+    E, intra = e.matrix(0, 1)
+    scale = np.abs(ref).max()
+    assert np.all(np.abs(E - ref) <= REL * np.abs(ref) + 1e-7 * scale), np.abs(E - ref).max()
+    tot_ref = np.triu(ref, 1).sum()
+    pot = e.replicas(0)["potential"]
+    assert np.all(np.abs(pot - tot_ref) <= REL * abs(tot_ref) + 1e-9)
+    # recompute into scratch leaves the state alone and agrees
+    assert np.allclose(e.recompute(False), pot, rtol=1e-12, atol=1e-12)
+
+
+def test_initial_energy_flexible_linker():
+    wl = workloads.make("c1")
+    sim = subset(wl, 2)
+    e = engine_for(wl, [sim])
+    o = oracle_for(wl, sim, mode=oracle.FP64)
+    pot = e.replicas(0)["potential"]
+    assert abs(pot[0] - o.initial_energy) <= REL * abs(o.initial_energy)
+
+
+def test_reference_flexible_replica_energy(refdata):
+    # tests/testReplica.cpp:79-82 through the engine: conf1, 1b residues 73-76 flexible
+    mols = []
+    for key, segs in (("conf1/1a", []), ("conf1/1b", [[72, 73, 74, 75]])):
+        rec = refdata["pdbs"][key]
+        aa = np.array([r["aa"] for r in rec["residues"]], np.int32)
+        mols.append(workloads.Molecule(np.array([r["xyz"] for r in rec["residues"]], np.float32), aa,
+                                       [refdata["amino_acids"][a]["charge"] for a in aa],
+                                       [refdata["amino_acids"][a]["radius"] for a in aa], segments=segs,
+                                       res_seq=[r["seq"] for r in rec["residues"]]))
+    sim = workloads.Simulation(mols, 118.4, [300.0], [0.5], [0.2])
+    V = np.array(refdata["torsion_V"])
+    S = np.array(refdata["torsion_sigma"])
+    wl = workloads.Workload("conf1", [sim], np.array(refdata["lj_table"], np.float32), V, S, seed=1)
+    e = eng.from_workload(wl, cluster=1)
+    pot = e.replicas(0)["potential"][0]
+    assert pot == pytest.approx(sum(refdata["kats"]["replica_flexible"]), rel=1.2e-5)
+    E, intra = e.matrix(0, 0)
+    assert E[0, 1] == pytest.approx(sum(refdata["kats"]["replica_rigid"]), rel=1.2e-5)
+
+
+def compare_runs(e, o, sim_index=0, pos_tol=2e-3):
+    R = o.R
+    rep = e.replicas(sim_index)
+    assert np.array_equal(rep["temperature"], o.temperature)
+    assert np.array_equal(rep["label"], o.label)
+    c = o.counters()
+    for k in ("accept", "acceptA", "reject", "totalAccept", "totalAcceptReject"):
+        assert np.array_equal(rep[k], c[k]), (k, rep[k], c[k])
+    assert np.all(np.abs(rep["potential"] - o.potential) <= REL * np.abs(o.potential) + 1e-6)
+    for r in range(R):
+        xyz, rel, cen = e.state(sim_index, r)
+        assert np.abs(xyz - o.pos[r]).max() < pos_tol
+        assert np.abs(cen - o.center[r]).max() < pos_tol
+
+
+@pytest.mark.parametrize("config,nrep,blocks,steps", [("c0", 4, 3, 100), ("c4", 4, 2, 60), ("c1", 4, 3, 100)])
+def test_trajectory_matches_oracle(config, nrep, blocks, steps):
+    wl = workloads.make(config)
+    sim = subset(wl, nrep)
+    e = engine_for(wl, [sim])
+    o = oracle_for(wl, sim)
+    e.run(blocks, steps, exchange_after_last=True)
+    orep, oex = o.run(blocks, steps, exchange_after_last=True)
+    compare_runs(e, o)
+    assert e.error_bits() == 0
+    # per-temperature reports and exchange counts of every exchange are identical
+    for b in range(blocks):
+        er, ex = e.report(0, b)
+        assert np.allclose(er, orep[b], equal_nan=True), (b, er, orep[b])
+        assert tuple(ex) == tuple(oex[b])
+
+
+@pytest.mark.parametrize("cluster", [2, 4])
+def test_cluster_split_matches_single_cta(cluster):
+    wl = workloads.make("c4")
+    sim = subset(wl, 3)
+    e1 = engine_for(wl, [sim], cluster=1)
+    ec = engine_for(wl, [sim], cluster=cluster)
+    assert ec.launch_shape()[0] == cluster
+    e1.run(2, 80)
+    ec.run(2, 80)
+    r1, rc = e1.replicas(0), ec.replicas(0)
+    for k in ("accept", "acceptA", "reject", "label"):
+        assert np.array_equal(r1[k], rc[k])
+    assert np.allclose(r1["potential"], rc["potential"], rtol=1e-9, atol=1e-9)
+    for r in range(3):
+        assert np.abs(e1.state(0, r)[0] - ec.state(0, r)[0]).max() < 1e-5
+
+
+def test_running_total_has_no_drift():
+    wl = workloads.make("c4")
+    sim = subset(wl, 4)
+    e = engine_for(wl, [sim], cluster=2)
+    e.run(5, 200)
+    run_tot = e.replicas(0)["potential"]
+    fresh = e.recompute(False)
+    assert np.allclose(run_tot, fresh, rtol=1e-9, atol=1e-9)
+    # and the state's energy agrees with the FP64 oracle on the engine's coordinates
+    for r in range(4):
+        xyz, _, _ = e.state(0, r)
+        ref = np.triu(oracle_matrix(wl, sim, xyz), 1).sum()
+        assert abs(run_tot[r] - ref) <= REL * abs(ref) + 1e-9
+
+
+def test_batched_simulations_match_separate_oracles():
+    # three small simulations of different shapes in one launch
+    wl0, wl4, wl1 = workloads.make("c0"), workloads.make("c4"), workloads.make("c1")
+    sims = [subset(wl0, 3), subset(wl4, 2)]
+    e = engine_for(wl0, sims)  # same contact table object is used for both
+    e.run(2, 50)
+    off = 0
+    for s, sim in enumerate(sims):
+        o = OracleRemc(sim.molecules, wl0.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
+                       sim.move_weights, sim.rigid_rotate_prob, None, None, seed=wl0.seed, rep_off=off, sim_index=s)
+        o.run(2, 50)
+        compare_runs(e, o, sim_index=s)
+        off += o.R
+
+
+def test_fraction_bound_sampling_matches_oracle():
+    wl = workloads.make("c4")
+    sim = subset(wl, 3)
+    e = engine_for(wl, [sim], sample_frequency=10, sample_after=0)
+    o = oracle_for(wl, sim, sample_frequency=10, sample_after=0)
+    e.run(2, 100, exchange_after_last=False)
+    o.run(2, 100, exchange_after_last=False)
+    rep = e.replicas(0)
+    c = o.counters()
+    for k in ("boundSamples", "samplesSinceLastExchange", "totalBoundSamples", "totalSamples"):
+        assert np.array_equal(rep[k], c[k]), k
+    e.final_report(1)
+    fo = o.final_report()
+    fe, _ = e.report(0, 1)
+    assert np.allclose(fe, fo, equal_nan=True)
+
+
+def test_counters_and_launches():
+    wl = workloads.make("c0")
+    sim = subset(wl, 2)
+    e = engine_for(wl, [sim])
+    e.run(3, 10)
+    steps, pairs = e.counters()
+    assert steps == 2 * 30
+    assert pairs == 2 * 30 * 76 * 76
+    assert e.last_launches() == 6
