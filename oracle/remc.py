@@ -259,6 +259,11 @@ class OracleRemc:
                                          _ptr(np.ascontiguousarray(self.pos[slot]), c_float), ctypes.byref(nc))
         return e, nc.value
 
+    def energy_of(self, xyz, mode=1):
+        """Total energy (kcal/mol) of arbitrary coordinates [N,3] of this system."""
+        x = np.ascontiguousarray(xyz, np.float32)
+        return self.L.oracle_replica_energy(ctypes.byref(self.sys), mode, _ptr(x, c_float), None)
+
     def counters(self):
         return {n: np.array([getattr(self.stats[i], n) for i in range(self.R)])
                 for n, _ in OracleStats._fields_ if n != "pad"}

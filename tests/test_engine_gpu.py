@@ -96,7 +96,11 @@ def test_reference_flexible_replica_energy(refdata):
     assert E[0, 1] == pytest.approx(sum(refdata["kats"]["replica_rigid"]), rel=1.2e-5)
 
 
-def compare_runs(e, o, sim_index=0, pos_tol=2e-3):
+def compare_runs(e, o, sim_index=0, pos_tol=2e-3, traj_rel=REL):
+    """Same decisions, same exchanges; coordinates within float drift; the engine's
+    running total within 1e-5 of the FP64 oracle evaluated on the engine's own
+    coordinates; the two totals within `traj_rel` of each other (they are energies of
+    coordinates that differ by the accumulated float rounding of the moves)."""
     R = o.R
     rep = e.replicas(sim_index)
     assert np.array_equal(rep["temperature"], o.temperature)
@@ -104,11 +108,13 @@ def compare_runs(e, o, sim_index=0, pos_tol=2e-3):
     c = o.counters()
     for k in ("accept", "acceptA", "reject", "totalAccept", "totalAcceptReject"):
         assert np.array_equal(rep[k], c[k]), (k, rep[k], c[k])
-    assert np.all(np.abs(rep["potential"] - o.potential) <= REL * np.abs(o.potential) + 1e-6)
+    assert np.all(np.abs(rep["potential"] - o.potential) <= traj_rel * np.abs(o.potential) + 1e-6)
     for r in range(R):
         xyz, rel, cen = e.state(sim_index, r)
         assert np.abs(xyz - o.pos[r]).max() < pos_tol
         assert np.abs(cen - o.center[r]).max() < pos_tol
+        e64 = o.energy_of(xyz, oracle.FP64)
+        assert abs(rep["potential"][r] - e64) <= REL * abs(e64) + 1e-9, (r, rep["potential"][r], e64)
 
 
 @pytest.mark.parametrize("config,nrep,blocks,steps", [("c0", 4, 3, 100), ("c4", 4, 2, 60), ("c1", 4, 3, 100)])
@@ -119,7 +125,7 @@ def test_trajectory_matches_oracle(config, nrep, blocks, steps):
     o = oracle_for(wl, sim)
     e.run(blocks, steps, exchange_after_last=True)
     orep, oex = o.run(blocks, steps, exchange_after_last=True)
-    compare_runs(e, o)
+    compare_runs(e, o, traj_rel=REL if config != "c1" else 2e-4)
     assert e.error_bits() == 0
     # per-temperature reports and exchange counts of every exchange are identical
     for b in range(blocks):
