@@ -158,7 +158,8 @@ def test_running_total_has_no_drift():
     e.run(5, 200)
     run_tot = e.replicas(0)["potential"]
     fresh = e.recompute(False)
-    assert np.allclose(run_tot, fresh, rtol=1e-9, atol=1e-9)
+    # a fresh evaluation sums each molecule pair from the other side: FP32-level noise only
+    assert np.allclose(run_tot, fresh, rtol=1e-6, atol=1e-7)
     # and the state's energy agrees with the FP64 oracle on the engine's coordinates
     for r in range(4):
         xyz, _, _ = e.state(0, r)
