@@ -404,3 +404,107 @@ int cgppd_last_energy_components(double *out3)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free variant
+//
+// Some hosts of this library cannot allocate device memory while they evaluate
+// energies: code that runs inside another framework's memory pool or under a fixed
+// device-memory budget, and callers that must not introduce allocation calls into a
+// timed or real-time loop.  CUDA_EonDevice_noalloc gives them the CUDA_EonDevice
+// result without any allocation: its scratch (CTA partials, completion ticket, error
+// flags, result slot) is a file-scope __device__ array, which every GPU that loads the
+// library holds until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxResidues = 16384;                       // datasetSize limit
+constexpr int kNoAllocMaxTiles = kNoAllocMaxResidues / kTile;    // 128-residue tiles
+constexpr int kNoAllocMaxCtas = kNoAllocMaxTiles * (kNoAllocMaxTiles + 1) / 2;
+// layout: [0] ticket, [4] flags, [256] result (3 doubles), [512] 2 doubles per CTA
+constexpr size_t kNoAllocBytes = 512 + 2 * sizeof(double) * kNoAllocMaxCtas;  // 132,608 bytes
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_addr[kMaxDevices] = {nullptr};  // device address of the array, per device
+
+// In host code g_noalloc_scratch names a host-side stand-in, not device memory; the
+// kernel needs the device address, looked up once per device with that device current.
+unsigned char *noalloc_scratch(int dev)
+{
+    if (dev < 0 || dev >= kMaxDevices) {
+        cgppd_fail("CUDA_EonDevice_noalloc: device ordinal above 63");
+        return nullptr;
+    }
+    if (g_noalloc_addr[dev] == nullptr) {
+        void *p = nullptr;
+        if (cgppd_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "CUDA_EonDevice_noalloc set-up") != 0)
+            return nullptr;
+        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    return g_noalloc_addr[dev];
+}
+
+}  // namespace
+
+extern "C" {
+
+// Same arguments and result as CUDA_EonDevice.  The first call on a device performs
+// the one-time set-up (the device address of the static scratch) and should come
+// before any stream capture.  datasetSize above 16384 residues is rejected with an
+// error (result 0).  Every call shares the one array and leaves the last call's data
+// in it; the ticket and error flags are cleared before each launch.  Two calls whose
+// kernels overlap on the GPU would race on the array: this function holds a
+// process-wide lock and returns only after its kernel and result copy have finished,
+// so calls made through it do not overlap.
+void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *residueCount,
+                            int *moleculePositions, int *moleculeCount, float *LJPotentials, double *result,
+                            int blockSize, int datasetSize, int sharedMemSize)
+{
+    (void)residueCount, (void)moleculePositions, (void)moleculeCount, (void)LJPotentials, (void)blockSize,
+        (void)sharedMemSize;
+    *result = 0.0;
+    if (datasetSize <= 0)
+        return;
+    if (datasetSize > kNoAllocMaxResidues) {
+        cgppd_fail("CUDA_EonDevice_noalloc: datasetSize exceeds the 16384-residue limit of its static scratch");
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    const int dev = current_device();
+    const float *table = nullptr;
+    {
+        std::lock_guard<std::mutex> tlock(g_mu);
+        table = bound_table();
+    }
+    if (table == nullptr) {
+        cgppd_fail("CUDA_EonDevice_noalloc: no contact table bound (call bindLJTexture first)");
+        return;
+    }
+    unsigned char *base = noalloc_scratch(dev);
+    if (base == nullptr)
+        return;
+    Scratch s;
+    s.ticket = reinterpret_cast<unsigned *>(base);
+    s.flags = reinterpret_cast<unsigned *>(base + 4);
+    s.result = reinterpret_cast<double *>(base + 256);
+    s.partials = reinterpret_cast<double *>(base + 512);
+    s.capacity = kNoAllocMaxCtas;
+    if (cgppd_check(cudaMemsetAsync(base, 0, 8, cudaStreamLegacy), "CUDA_EonDevice_noalloc clear") != 0)
+        return;
+    if (launch_energy(false, residuePositions, residueMeta, datasetSize, table, &s, nullptr, 0, cudaStreamLegacy) != 0)
+        return;
+    double host[3];
+    unsigned flags = 0;
+    if (cgppd_check(cudaMemcpy(host, s.result, sizeof(host), cudaMemcpyDeviceToHost), "CUDA_EonDevice_noalloc copy") != 0)
+        return;
+    if (cgppd_check(cudaMemcpy(&flags, s.flags, sizeof(flags), cudaMemcpyDeviceToHost), "CUDA_EonDevice_noalloc copy") != 0)
+        return;
+    if (flags != 0u) {
+        cgppd_fail("CUDA_EonDevice_noalloc: residue type index outside the 20x20 table");
+        return;
+    }
+    *result = host[2];
+}
+
+}  // extern "C"

@@ -63,6 +63,20 @@ void CUDA_freeBoxDimension(void);
 void bindLJTexture(float *ljp);
 void unbindLJTexture(void);
 
+/* No counterpart in the reference.  CUDA_EonDevice for callers that cannot allocate
+ * device memory while they evaluate energies (code running inside another
+ * framework's memory pool or under a fixed device-memory budget, or a loop that must
+ * stay free of allocation calls): same arguments and result, but its scratch is a
+ * static 132,608-byte device array owned by the library, so it calls no cudaMalloc or
+ * cudaFree.  datasetSize is limited to 16384 residues (larger sizes are rejected with
+ * an error and *result = 0).  The first call on a device looks up the array's device
+ * address (one-time set-up) and should come before any stream capture.  All calls
+ * share the array; calls whose kernels overlapped on the GPU would race, so this
+ * function serialises its own calls and returns after its kernel has finished. */
+void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *residueCount,
+                            int *moleculePositions, int *moleculeCount, float *LJPotentials, double *result,
+                            int blockSize, int datasetSize, int sharedMemSize);
+
 /* Library extension (no reference counterpart): {LJ raw, DH raw, total} of the last
  * synchronous call on the current device.  Returns 0 on success. */
 int cgppd_last_energy_components(double *out3);
