@@ -298,7 +298,7 @@ def gpu_arm(args):
             "config": {"workload": wl.name, "replicas": R, "mc_steps_per_bench_step": K,
                        "exchange": "after every block", "l2": "256 MiB flush before every timed step, inside the "
                                                              "timed region", "cluster_ctas_per_replica": shape[0],
-                       "threads_per_cta": shape[1], "parallelism": "replicas on one GPU" if world == 1 else
+                       "threads_per_cta": shape[1], "state_in_shared_memory": shape[2], "parallelism": "replicas on one GPU" if world == 1 else
                        "dp%d (independent replica sets)" % world},
             "pair_evals_per_s": pair_rate,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",

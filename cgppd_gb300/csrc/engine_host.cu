@@ -21,7 +21,7 @@
 #include "status.h"
 
 namespace cgppd {
-size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster);
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible);
 cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
                             cudaStream_t stream);
 cudaError_t set_mc_smem_limit(size_t smem);
@@ -106,6 +106,8 @@ struct cgppd_engine {
     size_t smem = 0;
     int total_replicas = 0;
     int max_n = 0, max_m = 0, max_mol = 0;
+    int resident = 0, any_flexible = 0;
+    int resident_pref = 1;
     int report_capacity = 0;
     int last_launches = 0;
 
@@ -192,6 +194,8 @@ struct cgppd_engine {
         a.max_n = max_n;
         a.max_m = max_m;
         a.max_mol = max_mol;
+        a.resident = resident;
+        a.any_flexible = any_flexible;
         return a;
     }
 
@@ -245,6 +249,13 @@ int cgppd_engine::build()
         ds.w1_cum[1] = (hs.p.move_weights[1] + hs.p.move_weights[2]) / w1;
         ds.w1_cum[2] = 1.0f;
         ds.rigid_rotate_p = hs.p.rigid_rotate_prob;
+        // u < c  <=>  w < ceil(c 2^32) for the 32-bit draw w = u 2^32
+        auto thr = [](float c) { return (unsigned long long)std::ceil((double)c * 4294967296.0); };
+        for (int k = 0; k < 4; ++k)
+            ds.thr4[k] = thr(ds.w_cum[k]);
+        for (int k = 0; k < 3; ++k)
+            ds.thr3[k] = thr(ds.w1_cum[k]);
+        ds.thr_rot = thr(ds.rigid_rotate_p);
         ds.sample_freq = hs.p.sample_frequency;
         ds.sample_after = hs.p.sample_after;
         ds.bound_threshold = hs.p.bound_threshold;
@@ -257,6 +268,8 @@ int cgppd_engine::build()
         for (int mi = 0; mi < M; ++mi) {
             HostMolecule &hm = hs.mols[mi];
             const bool flexible = !hs.p.rigid_only && (hm.all_flexible || !hm.segments.empty());
+            if (flexible)
+                any_flexible = 1;
             flexible_exists = flexible_exists || (hm.all_flexible || !hm.segments.empty());
             if (hm.crowder)
                 seen_crowder = true;
@@ -568,8 +581,11 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
             cluster *= 2;
     }
     e->cluster = std::min(8, std::max(1, cluster));
-    const size_t s_mc = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, e->cluster);
-    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1);
+    // keep each replica's state in shared memory when it fits (<= 160 KB per CTA)
+    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, e->cluster, 1, e->any_flexible);
+    e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024;
+    const size_t s_mc = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, e->cluster, e->resident, e->any_flexible);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
     e->smem = s_mc;
     if (std::max(s_mc, s_init) > 227 * 1024)
         return cgppd_fail("cgppd_engine_finalize: system too large for shared memory (reduce molecule size or N)");
@@ -705,7 +721,7 @@ int cgppd_engine_recompute(cgppd_engine *e, double *out, int write_state)
     if (cgppd_check(cudaStreamSynchronize(e->own_stream), "recompute") != 0)
         return -1;
     EngineArgs a = e->args();
-    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
     double *dst = write_state ? e->d_potential.ptr : e->d_scratch_pot.ptr;
     if (!write_state) {
         // evaluate into scratch copies so the running state is untouched
@@ -835,7 +851,7 @@ int cgppd_engine_upload(cgppd_engine *e, int sim, const float *pos4, const float
         rc |= cgppd_check(cudaMemcpyAsync(e->d_center.ptr + S.molst_off, centers4, sizeof(float4) * S.M * S.R,
                                           cudaMemcpyHostToDevice, st), "upload centres");
     if (rc == 0 && recompute) {
-        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1);
+        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
         rc |= cgppd_check(launch_init_energy(e->args(), e->total_replicas, s_init, e->d_potential.ptr, st),
                           "upload recompute");
     }
@@ -930,13 +946,21 @@ unsigned cgppd_engine_error_bits(cgppd_engine *e)
 
 int cgppd_engine_last_launches(const cgppd_engine *e) { return e->last_launches; }
 
+int cgppd_engine_set_resident(cgppd_engine *e, int allow)
+{
+    if (e->finalized)
+        return cgppd_fail("cgppd_engine_set_resident: engine already finalized");
+    e->resident_pref = allow ? 1 : 0;
+    return 0;
+}
+
 int cgppd_engine_launch_shape(const cgppd_engine *e, int *cluster, int *threads)
 {
     if (cluster)
         *cluster = e->cluster;
     if (threads)
         *threads = e->threads;
-    return 0;
+    return e->resident;
 }
 
 }  // extern "C"

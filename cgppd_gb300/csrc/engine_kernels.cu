@@ -1,6 +1,6 @@
 // engine_kernels.cu -- device side of the batched replica-exchange Monte Carlo engine.
 //
-// k_mc_block: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
+// k_mc<RES>: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
 // that replica with no inter-replica traffic (replicas are independent between
 // exchanges).  A step restates Replica::MCSearch (src/Replica.cpp:350-414):
 //   1. pick a molecule and a move (src/Molecule.cpp:451-504) from Philox draws,
@@ -14,10 +14,16 @@
 // The reference recomputes every pair each step; only the moved molecule's pairs
 // change, so the engine evaluates those and keeps the rest in the matrix.
 //
+// RES = true: every CTA copies its replica's state (coordinates, static residue
+// records, centres, pair matrix, row sums) into shared memory at launch, updates it in
+// place, and rank 0 writes it back at the end -- no global-memory latency on the step's
+// serial path.  RES = false (large systems): state stays in global memory (L2) and
+// rank 0 commits there.
+//
 // Within a cluster every CTA builds the same proposal (same draws, same arithmetic),
 // takes a slice of the other residues, and the per-molecule partial rows are summed
-// through distributed shared memory in a fixed order, so all CTAs take the same
-// Metropolis decision.  CTA rank 0 alone writes global state.
+// through distributed shared memory in a fixed rank order, so every CTA takes the same
+// Metropolis decision.
 //
 // k_exchange: one warp per simulation performs the even/odd temperature exchange of
 // Simulation::run (src/Simulation.cpp:770-795) and the per-temperature bookkeeping of
@@ -32,52 +38,67 @@ namespace cg = cooperative_groups;
 namespace cgppd {
 
 constexpr int kTableStride = 32;
+constexpr int kMaxThreads = 256;
+constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct MoveDesc {
     int m, start, n, type, kind;
     int ri, br_off, br_cnt;
-    int flexible, wrapped, null_move;
+    int flexible, wrapped, null_move, nintra;
     float R[9];
     float vx, vy, vz;        // translation of the molecule (translate) or of residue ri (local)
-    float fx, fy, fz;        // v / n (local translate)
+    float fx, fy, fz;        // displacement / n (local, flex)
     float cx, cy, cz;        // centre before the move
     float wcx, wcy, wcz;     // centre after the move (wrapped)
     float px, py, pz;        // flex pivot position
-    double u_metro;
+    uint32_t w_metro;
 };
 
 struct SmemLayout {
-    // byte offsets into dynamic shared memory
-    int table, ipos, irel, iq, iexcl, idisp, ej, rowp, row, total;
+    int table, mols, ipos, irel, iexcl, idisp, iq, ej, rowp, row;    // always
+    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM;                        // resident only
+    int total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int max_m)
+__host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
+
+__host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int max_m, int max_n, int resident,
+                                                  int any_flexible)
 {
     SmemLayout L;
     int off = 0;
-    L.table = off; off += kTableStride * kTableStride * 4;
-    L.ipos = off;  off += 16 * max_mol;
-    L.irel = off;  off += 16 * max_mol;
-    L.iexcl = off; off += 16 * max_mol;
-    L.idisp = off; off += 16 * max_mol;
-    L.iq = off;    off += 8 * max_mol;
-    L.ej = off;    off += 8 * slice;
-    off = (off + 7) & ~7;
-    L.rowp = off;  off += 8 * (max_m + 1);
-    L.row = off;   off += 8 * (max_m + 1);
+    L.table = off;  off += kTableStride * kTableStride * 4;
+    L.mols = off;   off = align16(off + (int)sizeof(DevMol) * max_m);
+    L.ipos = off;   off += 16 * max_mol;
+    L.irel = off;   off += 16 * max_mol;
+    L.iexcl = off;  off += 16 * max_mol;
+    L.idisp = off;  off += 16 * max_mol;
+    L.iq = off;     off = align16(off + 8 * max_mol);
+    L.ej = off;     off = align16(off + 8 * slice);
+    L.rowp = off;   off = align16(off + 8 * (max_m + 1));
+    L.row = off;    off = align16(off + 8 * (max_m + 1));
+    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = 0;
+    if (resident) {
+        L.P = off;      off += 16 * max_n;
+        L.Q = off;      off += 16 * max_n;
+        L.ST = off;     off += 16 * max_n;
+        L.EX = off;     off += any_flexible ? 16 * max_n : 0;
+        L.CEN = off;    off += 16 * max_m;
+        L.EM = off;     off = align16(off + 8 * max_m * max_m);
+        L.INTRA = off;  off = align16(off + 8 * max_m);
+        L.ROWSUM = off; off = align16(off + 8 * max_m);
+    }
     L.total = off;
     return L;
 }
 
-size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster)
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible)
 {
-    int slice = (max_n + cluster - 1) / cluster;
-    return (size_t)smem_layout(max_mol, slice, max_m).total;
+    const int slice = (max_n + cluster - 1) / cluster;
+    return (size_t)smem_layout(max_mol, slice, max_m, max_n, resident, any_flexible).total;
 }
 
 // ------------------------------------------------------------------ helpers
-
-__device__ __forceinline__ FF ff_make(float hi, float lo) { return FF{hi, lo}; }
 
 __device__ __forceinline__ void ff_add_ff(FF &a, FF b)
 {
@@ -106,19 +127,19 @@ __device__ __forceinline__ double warp_sum_d(double v)
     return v;
 }
 
-// Block-wide double sum in a fixed order; result valid in every thread.
-__device__ double block_sum_d(double v, double *red)
+// Block-wide FF sum in a fixed order, returned as double in every thread.
+__device__ double block_sum_ff(FF v, FF *red)
 {
     const int t = threadIdx.x, nw = blockDim.x >> 5;
-    v = warp_sum_d(v);
+    v = ff_warp_sum(v);
     __syncthreads();
     if ((t & 31) == 0)
         red[t >> 5] = v;
     __syncthreads();
-    double s = 0.0;
+    FF s{0.f, 0.f};
     for (int w = 0; w < nw; ++w)
-        s += red[w];
-    return s;
+        ff_add_ff(s, red[w]);
+    return ff_value(s);
 }
 
 __device__ __forceinline__ float3 rot_apply(const float *R, float x, float y, float z)
@@ -127,55 +148,49 @@ __device__ __forceinline__ float3 rot_apply(const float *R, float x, float y, fl
                        fmaf(R[6], x, fmaf(R[7], y, R[8] * z)));
 }
 
-// Rotation matrix of quaternion (w, x, y, z), coefficients in double as
-// Quaternion::rotateVector forms them (src/Quaternion.cpp:95-112), stored as float.
-__device__ void quat_to_matrix(double w, double x, double y, double z, float *R)
+// Rotation matrix of the quaternion (cos(a/2), sin(a/2) axis) (src/Quaternion.cpp:12-21,
+// :95-112), optionally normalised first (Quaternion::normalize, :30-38).
+__device__ void axis_angle_matrix(float angle, float ax, float ay, float az, bool normalize, float *R)
 {
-    double w2 = w * w, x2 = x * x, y2 = y * y, z2 = z * z;
-    double wx = w * x, wy = w * y, wz = w * z, xy = x * y, xz = x * z, yz = y * z;
-    R[0] = (float)(w2 + x2 - y2 - z2);
-    R[1] = (float)((xy - wz) * 2.0);
-    R[2] = (float)((wy + xz) * 2.0);
-    R[3] = (float)((wz + xy) * 2.0);
-    R[4] = (float)(w2 - x2 + y2 - z2);
-    R[5] = (float)((yz - wx) * 2.0);
-    R[6] = (float)((xz - wy) * 2.0);
-    R[7] = (float)((yz + wx) * 2.0);
-    R[8] = (float)(w2 - x2 - y2 + z2);
-}
-
-// Quaternion(angle, axis) (src/Quaternion.cpp:12-21), optionally normalised
-// (Quaternion::normalize, :30-38), into a rotation matrix.
-__device__ void axis_angle_matrix(double angle, double ax, double ay, double az, bool normalize, float *R)
-{
-    double s, c;
-    sincos(angle / 2.0, &s, &c);
-    double w = c, x = s * ax, y = s * ay, z = s * az;
+    float s, c;
+    sincosf(0.5f * angle, &s, &c);
+    float w = c, x = s * ax, y = s * ay, z = s * az;
     if (normalize) {
-        double mag = sqrt(w * w + x * x + y * y + z * z);
-        w /= mag;
-        x /= mag;
-        y /= mag;
-        z /= mag;
+        const float inv = 1.0f / sqrtf(w * w + x * x + y * y + z * z);
+        w *= inv, x *= inv, y *= inv, z *= inv;
     }
-    quat_to_matrix(w, x, y, z, R);
+    const float w2 = w * w, x2 = x * x, y2 = y * y, z2 = z * z;
+    const float wx = w * x, wy = w * y, wz = w * z, xy = x * y, xz = x * z, yz = y * z;
+    R[0] = w2 + x2 - y2 - z2;
+    R[1] = (xy - wz) * 2.0f;
+    R[2] = (wy + xz) * 2.0f;
+    R[3] = (wz + xy) * 2.0f;
+    R[4] = w2 - x2 + y2 - z2;
+    R[5] = (yz - wx) * 2.0f;
+    R[6] = (xz - wy) * 2.0f;
+    R[7] = (yz + wx) * 2.0f;
+    R[8] = w2 - x2 - y2 + z2;
 }
 
 // Molecule::wrapped_centre: fmod per component (keeps the sign).
 __device__ __forceinline__ float wrapf(float c, float box) { return fmodf(c, box); }
 
-__device__ __forceinline__ int pick(double u, int n)
+// floor(u * n) for u = w / 2^32, exactly.
+__device__ __forceinline__ int pickw(uint32_t w, int n) { return (int)(((unsigned long long)w * (unsigned)n) >> 32); }
+
+// The draw u - 0.5 (or 0.5 - u) rounded once to float, exactly as (float)(u - 0.5).
+__device__ __forceinline__ float centred(uint32_t w, bool negate)
 {
-    int k = (int)(u * (double)n);
-    return k < n ? k : n - 1;
+    const long long d = negate ? (2147483648LL - (long long)w) : ((long long)w - 2147483648LL);
+    return (float)d * 2.3283064365386963e-10f;
 }
 
-__device__ __forceinline__ int discrete(double u, const float *cum, int n)
+__device__ __forceinline__ float3 normalized(float x, float y, float z)
 {
-    for (int k = 0; k < n - 1; ++k)
-        if (u < (double)cum[k])
-            return k;
-    return n - 1;
+    const float mag = sqrtf(x * x + y * y + z * z);
+    if (mag != 0.0f)
+        return make_float3(x / mag, y / mag, z / mag);
+    return make_float3(x, y, z);
 }
 
 // Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with
@@ -194,40 +209,109 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
     return lj + dh_term(qa.x * qb.x, r, inv_r);
 }
 
+__device__ __forceinline__ bool intra_excluded(int4 ei, int4 ej)
+{
+    // same rigid domain, backbone neighbours (|resSeq| < 4 on one chain), or bonded
+    // across a segment (src/Molecule.cpp:655, src/Residue.cpp:101-114)
+    return (ei.z != 0 && ei.z == ej.z) || (ei.x == ej.x && abs(ei.y - ej.y) < 4) || (ei.w != 0 && ei.w == ej.w);
+}
+
+// Bonded terms of one molecule at coordinates `p` (kcal/mol), thread-strided from
+// `t0` with stride `stride` (src/Potential.cpp:45-98 with Potential::total's factors).
+__device__ void bonded_terms(const EngineArgs &a, const DevMol &mol, const float4 *p, float L, float invL, int t0,
+                             int stride, FF &acc)
+{
+    for (int k = t0; k < mol.nbond; k += stride) {
+        const int2 b = a.bonds[mol.bond_off + k];
+        const float4 pi = p[b.x], pj = p[b.y];
+        const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
+                    dz = min_image(pj.z - pi.z, L, invL);
+        const float rr = sqrtf(dx * dx + dy * dy + dz * dz) - kR0;
+        ff_add(acc, 0.5f * kKSpring * rr * rr);
+    }
+    for (int k = t0; k < mol.nang; k += stride) {
+        const int4 an = a.angles[mol.ang_off + k];
+        const float4 pi = p[an.x], pj = p[an.y], pk = p[an.z];
+        const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
+        const float cbx = pk.x - pj.x, cby = pk.y - pj.y, cbz = pk.z - pj.z;
+        const float cm = sqrtf(cbx * cbx + cby * cby + cbz * cbz) * sqrtf(abx * abx + aby * aby + abz * abz);
+        float th = 0.f;
+        if (cm >= 1e-26f)
+            th = acosf(fminf(1.f, fmaxf(-1.f, (abx * cbx + aby * cby + abz * cbz) / cm)));
+        const float da = th - kThetaAlpha, db = th - kThetaBeta;
+        const float term =
+            expf(-kGammaAngle * (kKAlpha * da * da + kEpsAlpha)) + expf(-kGammaAngle * (kKBeta * db * db));
+        ff_add(acc, -kGammaAngleRecip * logf(term));
+    }
+    for (int k = t0; k < mol.ntor; k += stride) {
+        const int4 tq = a.tors[mol.tor_off + k];
+        const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
+        const float4 p1 = p[tq.x], p2 = p[tq.y], p3 = p[tq.z], p4 = p[tq.w];
+        const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
+        const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
+        const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
+        const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
+        const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
+        const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
+        const float phi =
+            atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), c12x * c23x + c12y * c23y + c12z * c23z);
+        const float e = V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
+                        V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
+        ff_add(acc, e);
+    }
+}
+
 // ------------------------------------------------------------------ move decision
 
-__device__ void decide_move(const EngineArgs &a, const DevSim &S, int g, int r, const uint32_t *w, MoveDesc &mv)
+// Loads of mutable state: plain shared-memory loads when resident, L2 loads otherwise
+// (another CTA of the cluster may have committed them).
+template <bool RES, typename T>
+__device__ __forceinline__ T ld_state(const T *p)
+{
+    if (RES)
+        return *p;
+    return __ldcg(p);
+}
+
+template <bool RES>
+__device__ void decide_move(const EngineArgs &a, const DevSim &S, const DevMol *mols, const float4 *CEN,
+                            const float4 *P, float tstep, float rstep, const uint32_t *w, MoveDesc &mv)
 {
     const int M = S.M;
-    mv.m = pick(u01(w[0]), M);
-    const DevMol mol = a.mols[S.mol_off + mv.m];
+    mv.m = pickw(w[0], M);
+    const DevMol mol = mols[mv.m];
     mv.start = mol.start;
     mv.n = mol.count;
     mv.flexible = (mol.flags & kMolFlexible) != 0;
+    mv.nintra = mol.nintra;
     mv.null_move = 0;
     mv.wrapped = 0;
     const float box = S.box;
-    const float4 c = __ldcg(&a.center[S.molst_off + (long long)r * M + mv.m]);
+    const float4 c = ld_state<RES>(&CEN[mv.m]);
     mv.cx = c.x, mv.cy = c.y, mv.cz = c.z;
     mv.wcx = c.x, mv.wcy = c.y, mv.wcz = c.z;
-    const double u1 = u01(w[1]);
-    if (mv.flexible)
-        mv.type = (M > 1) ? discrete(u1, S.w_cum, 4) : 1 + discrete(u1, S.w1_cum, 3);
-    else
-        mv.type = (u1 < (double)S.rigid_rotate_p) ? kRotate : kTranslate;  // gsl_ran_bernoulli
-    const double dx = u01(w[2]) - 0.5, dy = 0.5 - u01(w[3]), dz = u01(w[4]) - 0.5;
-    const float tstep = a.tstep[g];
-    const double rstep = a.rstep[g];
-    const long long base = S.state_off + (long long)r * S.N + mv.start;
+    if (mv.flexible) {
+        int k = 0;
+        if (M > 1) {
+            while (k < 3 && (unsigned long long)w[1] >= S.thr4[k])
+                ++k;
+            mv.type = k;
+        } else {
+            while (k < 2 && (unsigned long long)w[1] >= S.thr3[k])
+                ++k;
+            mv.type = 1 + k;
+        }
+    } else {
+        mv.type = ((unsigned long long)w[1] < S.thr_rot) ? kRotate : kTranslate;  // gsl_ran_bernoulli
+    }
+    const float dx = centred(w[2], false), dy = centred(w[3], true), dz = centred(w[4], false);
+    const float4 *Pm = P + mv.start;
 
     switch (mv.type) {
     case kTranslate: {
         // Molecule::translate(rng, step) (src/Molecule.cpp:146-159, :262-266)
-        float x = (float)dx, y = (float)dy, z = (float)dz;
-        float mag = sqrtf(x * x + y * y + z * z);
-        if (mag != 0.0f)
-            x /= mag, y /= mag, z /= mag;
-        mv.vx = x * tstep, mv.vy = y * tstep, mv.vz = z * tstep;
+        const float3 u = normalized(dx, dy, dz);
+        mv.vx = u.x * tstep, mv.vy = u.y * tstep, mv.vz = u.z * tstep;
         mv.wcx = wrapf(c.x + mv.vx, box);
         mv.wcy = wrapf(c.y + mv.vy, box);
         mv.wcz = wrapf(c.z + mv.vz, box);
@@ -235,8 +319,8 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, int g, int r, 
     }
     case kRotate: {
         // Molecule::rotate(rng, step) -> setRotation (src/Molecule.cpp:193-208, :255-260)
-        double mag = sqrt(dx * dx + dy * dy + dz * dz);
-        axis_angle_matrix(rstep, dx / mag, dy / mag, dz / mag, true, mv.R);
+        const float3 u = normalized(dx, dy, dz);
+        axis_angle_matrix(rstep, u.x, u.y, u.z, true, mv.R);
         break;
     }
     case kFlex: {
@@ -245,57 +329,53 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, int g, int r, 
             mv.null_move = 1;
             break;
         }
-        double mag = sqrt(dx * dx + dy * dy + dz * dz);
-        axis_angle_matrix(rstep, dx / mag, dy / mag, dz / mag, false, mv.R);
-        const int4 fr = a.flexres[mol.flex_off + pick(u01(w[5]), mol.nflex)];
+        const float3 u = normalized(dx, dy, dz);
+        axis_angle_matrix(rstep, u.x, u.y, u.z, false, mv.R);
+        const int4 fr = a.flexres[mol.flex_off + pickw(w[5], mol.nflex)];
         if (fr.y <= 0) {
             mv.null_move = 1;
             break;
         }
-        const int4 op = a.flexopt[fr.z + pick(u01(w[6]), fr.y)];
+        const int4 op = a.flexopt[fr.z + pickw(w[6], fr.y)];
         mv.ri = fr.x;
         mv.br_off = op.y;
         mv.br_cnt = op.z;
-        const float4 p = __ldcg(&a.pos[base + fr.x]);
+        const float4 p = ld_state<RES>(&Pm[fr.x]);
         mv.px = p.x, mv.py = p.y, mv.pz = p.z;
         break;
     }
     case kLocal: {
         // Molecule::make_local_moves (src/Molecule.cpp:415-448): Bernoulli(0.5) picks a
         // crankshaft (1) or a local translation (0) of one residue.
-        mv.kind = (u01(w[5]) < 0.5) ? 1 : 0;
+        mv.kind = (w[5] < 2147483648u) ? 1 : 0;
         float vx, vy, vz;
         if (mv.kind == 0) {
             if (mol.nlocal == 0) {
                 mv.null_move = 1;
                 break;
             }
-            mv.ri = a.localres[mol.local_off + pick(u01(w[6]), mol.nlocal)];
-            float x = (float)dx, y = (float)dy, z = (float)dz;
-            float mag = sqrtf(x * x + y * y + z * z);
-            if (mag != 0.0f)
-                x /= mag, y /= mag, z /= mag;
-            const double s = (double)0.1f * (double)tstep;
-            vx = (float)(x * s), vy = (float)(y * s), vz = (float)(z * s);
+            mv.ri = a.localres[mol.local_off + pickw(w[6], mol.nlocal)];
+            const float3 u = normalized(dx, dy, dz);
+            const float s = (float)((double)0.1f * (double)tstep);
+            vx = u.x * s, vy = u.y * s, vz = u.z * s;
         } else {
             if (mol.ncrank == 0) {
                 mv.null_move = 1;
                 break;
             }
-            int ri = a.crankres[mol.crank_off + pick(u01(w[6]), mol.ncrank)];
+            const int ri = a.crankres[mol.crank_off + pickw(w[6], mol.ncrank)];
             if (ri < 1 || ri + 1 >= mv.n) {  // needs both backbone neighbours in the array
                 mv.null_move = 1;
                 break;
             }
             mv.ri = ri;
-            const bool flip = u01(w[7]) < 0.5;
-            const float4 pm = __ldcg(&a.pos[base + ri - 1]);
-            const float4 p0 = __ldcg(&a.pos[base + ri]);
-            const float4 pp = __ldcg(&a.pos[base + ri + 1]);
-            double ax = (double)(pp.x - pm.x), ay = (double)(pp.y - pm.y), az = (double)(pp.z - pm.z);
-            double amag = sqrt(ax * ax + ay * ay + az * az);
+            const bool flip = w[7] < 2147483648u;
+            const float4 pm = ld_state<RES>(&Pm[ri - 1]);
+            const float4 p0 = ld_state<RES>(&Pm[ri]);
+            const float4 pp = ld_state<RES>(&Pm[ri + 1]);
+            const float3 ax = normalized(pp.x - pm.x, pp.y - pm.y, pp.z - pm.z);
             float Rm[9];
-            axis_angle_matrix(flip ? -rstep : rstep, ax / amag, ay / amag, az / amag, true, Rm);
+            axis_angle_matrix(flip ? -rstep : rstep, ax.x, ax.y, ax.z, true, Rm);
             const float3 rr = rot_apply(Rm, p0.x - pm.x, p0.y - pm.y, p0.z - pm.z);
             vx = (rr.x + pm.x) - p0.x;
             vy = (rr.y + pm.y) - p0.y;
@@ -314,19 +394,22 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, int g, int r, 
         break;
     }
     }
-    mv.u_metro = u01(w[8]);
+    mv.w_metro = w[8];
 }
 
 // ------------------------------------------------------------------ MC kernel
 
-__global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
+template <bool RES>
+__global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ MoveDesc mv;
-    __shared__ uint32_t s_w[12];
-    __shared__ double s_red[32];
-    __shared__ double s_old_row, s_pot, s_intrap, s_intra_new;
+    __shared__ FF s_red[kMaxWarps];
+    __shared__ float s_fred[3 * kMaxWarps];
+    __shared__ double s_old_row, s_pot, s_intrap, s_intra_new, s_new_row;
     __shared__ int s_accept;
+    __shared__ DevSim S;           // this replica's simulation (read by thread 0 mostly)
+    __shared__ ReplicaStats st;    // counters, updated by thread 0
 
     const int C = a.cluster;
     const int t = threadIdx.x, T = blockDim.x, lane = t & 31, warp = t >> 5, NW = T >> 5;
@@ -335,12 +418,17 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
         rank = (int)cg::this_cluster().block_rank();
     const int g = blockIdx.x / C;
     const int s = a.rep_sim[g];
-    const DevSim S = a.sims[s];
+    if (t == 0) {
+        S = a.sims[s];
+        st = a.stats[g];
+    }
+    __syncthreads();
     const int r = g - S.rep_off;
     const int N = S.N, M = S.M;
     const int slice = (a.max_n + C - 1) / C;
-    const SmemLayout Ly = smem_layout(a.max_mol, slice, a.max_m);
+    const SmemLayout Ly = smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible);
     float *s_table = reinterpret_cast<float *>(smem + Ly.table);
+    DevMol *s_mols = reinterpret_cast<DevMol *>(smem + Ly.mols);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
     float4 *s_irel = reinterpret_cast<float4 *>(smem + Ly.irel);
     int4 *s_iexcl = reinterpret_cast<int4 *>(smem + Ly.iexcl);
@@ -350,65 +438,122 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
     double *s_rowp = reinterpret_cast<double *>(smem + Ly.rowp);
     double *s_row = reinterpret_cast<double *>(smem + Ly.row);
 
+    const long long st0 = S.state_off + (long long)r * N;
+    float4 *gP = a.pos + st0;
+    float4 *gQ = a.rel + st0;
+    float4 *gCEN = a.center + S.molst_off + (long long)r * M;
+    double *gE = a.emat + S.emat_off + (long long)r * M * M;
+    double *gINTRA = a.intra + S.molst_off + (long long)r * M;
+    const float4 *gST = a.rstat + S.res_off;
+    const int4 *gEX = a.rexcl + S.res_off;
+
+    // state views: shared-memory copies when resident, global memory otherwise
+    float4 *P = RES ? reinterpret_cast<float4 *>(smem + Ly.P) : gP;
+    float4 *Q = RES ? reinterpret_cast<float4 *>(smem + Ly.Q) : gQ;
+    const float4 *ST = RES ? reinterpret_cast<const float4 *>(smem + Ly.ST) : gST;
+    const int4 *EX = (RES && a.any_flexible) ? reinterpret_cast<const int4 *>(smem + Ly.EX) : gEX;
+    float4 *CEN = RES ? reinterpret_cast<float4 *>(smem + Ly.CEN) : gCEN;
+    double *EM = RES ? reinterpret_cast<double *>(smem + Ly.EM) : gE;
+    double *INTRA = RES ? reinterpret_cast<double *>(smem + Ly.INTRA) : gINTRA;
+    double *ROWSUM = RES ? reinterpret_cast<double *>(smem + Ly.ROWSUM) : nullptr;
+
     for (int k = t; k < kTableStride * kTableStride; k += T)
         s_table[k] = a.table[k];
+    for (int k = t; k < M; k += T)
+        s_mols[k] = a.mols[S.mol_off + k];
+    if (RES) {
+        float4 *sP = P, *sQ = Q, *sC = CEN;
+        float4 *sST = reinterpret_cast<float4 *>(smem + Ly.ST);
+        for (int i = t; i < N; i += T) {
+            sP[i] = __ldcg(&gP[i]);
+            sQ[i] = __ldcg(&gQ[i]);
+            sST[i] = gST[i];
+        }
+        if (a.any_flexible) {
+            int4 *sEX = reinterpret_cast<int4 *>(smem + Ly.EX);
+            for (int i = t; i < N; i += T)
+                sEX[i] = gEX[i];
+        }
+        for (int k = t; k < M; k += T) {
+            sC[k] = __ldcg(&gCEN[k]);
+            INTRA[k] = __ldcg(&gINTRA[k]);
+        }
+        for (int k = t; k < M * M; k += T)
+            EM[k] = __ldcg(&gE[k]);
+        __syncthreads();
+        // row sums: S[m] = intra[m] + sum_b E[m][b]
+        for (int k = t; k < M; k += T) {
+            double v = INTRA[k];
+            for (int b = 0; b < M; ++b)
+                if (b != k)
+                    v += EM[(long long)k * M + b];
+            ROWSUM[k] = v;
+        }
+    }
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
-    const long long st0 = S.state_off + (long long)r * N;
-    const float4 *stat = a.rstat + S.res_off;
-    const int4 *excl = a.rexcl + S.res_off;
-    double *E = a.emat + S.emat_off + (long long)r * M * M;
-    double *intra = a.intra + S.molst_off + (long long)r * M;
-    float4 *centers = a.center + S.molst_off + (long long)r * M;
+    const float tstep = a.tstep[g];
+    const float rstep = (float)a.rstep[g];
+    const float temperature = a.temperature[g];
     const uint32_t key0 = a.seed_lo ^ (0x9E3779B9u * (uint32_t)(g + 1)), key1 = a.seed_hi;
+    const unsigned long long step0 = a.stepc[g];
+    // pair and error counters live in registers of thread 0 (rank 0 writes them back)
+    unsigned long long pairs = 0;
+    unsigned errbits = 0;
+    if (t == 0)
+        s_pot = __ldcg(&a.potential[g]);
     __syncthreads();
 
-    const unsigned long long step0 = a.stepc[g];
     for (int step = 0; step < nsteps; ++step) {
         const unsigned long long mcstep = step0 + (unsigned long long)step;
-        // ---- draws and move decision (thread 0 of every CTA computes the same)
-        if (t < 3) {
-            U4 ctr{(uint32_t)mcstep, (uint32_t)(mcstep >> 32), (uint32_t)t, 0x4D43u};
-            U4 o = philox4x32_10(ctr, key0, key1);
-            s_w[4 * t + 0] = o.x;
-            s_w[4 * t + 1] = o.y;
-            s_w[4 * t + 2] = o.z;
-            s_w[4 * t + 3] = o.w;
+        // ---- draws (lanes 0-2 of warp 0) and the move decision (thread 0)
+        if (warp == 0) {
+            uint32_t o[4] = {0u, 0u, 0u, 0u};
+            if (lane < 3) {
+                const U4 ctr{(uint32_t)mcstep, (uint32_t)(mcstep >> 32), (uint32_t)lane, 0x4D43u};
+                const U4 res = philox4x32_10(ctr, key0, key1);
+                o[0] = res.x, o[1] = res.y, o[2] = res.z, o[3] = res.w;
+            }
+            uint32_t w[12];
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    w[4 * b + k] = __shfl_sync(0xffffffffu, o[k], b);
+            if (lane == 0) {
+                decide_move<RES>(a, S, s_mols, CEN, P, tstep, rstep, w, mv);
+                s_old_row = RES ? ROWSUM[mv.m] : 0.0;
+            }
         }
         __syncthreads();
-        if (t == 0)
-            decide_move(a, S, g, r, s_w, mv);
-        __syncthreads();
-        const int n = mv.n, start = mv.start, type = mv.type;
+        const int n = mv.n, start = mv.start, type = mv.type, m = mv.m;
         const bool nullm = mv.null_move != 0;
         const bool flexmol = mv.flexible != 0;
 
-        // ---- old row (read before anyone commits this step)
-        if (warp == 0) {
+        if (!RES && warp == 0) {
+            // old row from the global matrix (read before anyone commits this step)
             double v = 0.0;
             for (int b = lane; b < M; b += 32)
-                if (b != mv.m)
-                    v += __ldcg(&E[(long long)mv.m * M + b]);
+                if (b != m)
+                    v += __ldcg(&EM[(long long)m * M + b]);
             v = warp_sum_d(v);
-            if (lane == 0) {
-                s_old_row = v + __ldcg(&intra[mv.m]);
-                s_pot = __ldcg(&a.potential[g]);
-            }
+            if (lane == 0)
+                s_old_row = v + __ldcg(&INTRA[m]);
         }
 
         // ---- proposal of the moved molecule
         for (int i = t; i < n; i += T) {
-            const float4 p = __ldcg(&a.pos[st0 + start + i]);
-            const float4 q = __ldcg(&a.rel[st0 + start + i]);
-            const float4 sr = __ldg(&stat[start + i]);
+            const float4 p = ld_state<RES>(&P[start + i]);
+            const float4 q = ld_state<RES>(&Q[start + i]);
+            const float4 sr = ST[start + i];
             s_iq[i] = make_float2(sr.y, sr.z);
             if (flexmol)
-                s_iexcl[i] = __ldg(&excl[start + i]);
+                s_iexcl[i] = EX[start + i];
             float4 np = p, nq = q;
             if (!nullm) {
                 if (type == kTranslate) {
                     np = make_float4(q.x + mv.wcx, q.y + mv.wcy, q.z + mv.wcz, 0.f);
                 } else if (type == kRotate) {
-                    float3 rr = rot_apply(mv.R, q.x, q.y, q.z);
+                    const float3 rr = rot_apply(mv.R, q.x, q.y, q.z);
                     nq = make_float4(rr.x, rr.y, rr.z, 0.f);
                     np = make_float4(mv.cx + rr.x, mv.cy + rr.y, mv.cz + rr.z, 0.f);
                 } else if (type == kLocal) {
@@ -449,15 +594,15 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
                 sz += __shfl_xor_sync(0xffffffffu, sz, o);
             }
             if (lane == 0) {
-                s_red[3 * warp + 0] = sx;  // s_red holds doubles; floats stored exactly
-                s_red[3 * warp + 1] = sy;
-                s_red[3 * warp + 2] = sz;
+                s_fred[3 * warp + 0] = sx;
+                s_fred[3 * warp + 1] = sy;
+                s_fred[3 * warp + 2] = sz;
             }
             __syncthreads();
             if (t == 0) {
                 float ax = 0.f, ay = 0.f, az = 0.f;
                 for (int w = 0; w < NW; ++w)
-                    ax += (float)s_red[3 * w], ay += (float)s_red[3 * w + 1], az += (float)s_red[3 * w + 2];
+                    ax += s_fred[3 * w], ay += s_fred[3 * w + 1], az += s_fred[3 * w + 2];
                 const float nf = (float)n;
                 mv.fx = ax / nf, mv.fy = ay / nf, mv.fz = az / nf;
                 const float ncx = mv.cx + mv.fx, ncy = mv.cy + mv.fy, ncz = mv.cz + mv.fz;
@@ -497,8 +642,8 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
             FF acc{0.f, 0.f};
             if (valid) {
                 const int j = (o < start) ? o : o + n;
-                const float4 pj = __ldcg(&a.pos[st0 + j]);
-                const float4 sj = __ldg(&stat[j]);
+                const float4 pj = ld_state<RES>(&P[j]);
+                const float4 sj = ST[j];
                 const float4 rj = make_float4(pj.x, pj.y, pj.z, sj.x);
                 const float2 qj = make_float2(sj.y, sj.z);
                 float part = 0.f;
@@ -540,73 +685,29 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
                     const float2 qj = s_iq[j];
                     const int4 ej = s_iexcl[j];
                     const int iend = (ta == tb) ? j : min(n, ta * 32 + 32);
-                    for (int i = ta * 32; i < iend; ++i) {
-                        const int4 ei = s_iexcl[i];
-                        const bool ex = (ei.z != 0 && ei.z == ej.z) || (ei.x == ej.x && abs(ei.y - ej.y) < 4) ||
-                                        (ei.w != 0 && ei.w == ej.w);
-                        if (!ex)
+                    for (int i = ta * 32; i < iend; ++i)
+                        if (!intra_excluded(s_iexcl[i], ej))
                             part += pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
-                    }
                 }
                 ff_add(iacc, part);
             }
             if (rank == 0) {
-                const DevMol mol = a.mols[S.mol_off + mv.m];
+                const DevMol &mol = s_mols[m];
                 // indirect neighbours not caught by the rules above
                 for (int k = t; k < mol.nind; k += T) {
                     const int2 pr = a.indsub[mol.ind_off + k];
                     ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
                 }
-                // bonds: 0.5 K (r - R0)^2 with the minimum-image distance
-                for (int k = t; k < mol.nbond; k += T) {
-                    const int2 b = a.bonds[mol.bond_off + k];
-                    const float4 pi = s_ipos[b.x], pj = s_ipos[b.y];
-                    const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
-                                dz = min_image(pj.z - pi.z, L, invL);
-                    const float rr = sqrtf(dx * dx + dy * dy + dz * dz) - kR0;
-                    ff_add(iacc, 0.5f * kKSpring * rr * rr);
-                }
-                // angles: -(1/gamma) log(exp(-gamma(ka(t-ta)^2 + ea)) + exp(-gamma kb (t-tb)^2))
-                for (int k = t; k < mol.nang; k += T) {
-                    const int4 an = a.angles[mol.ang_off + k];
-                    const float4 pi = s_ipos[an.x], pj = s_ipos[an.y], pk = s_ipos[an.z];
-                    const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
-                    const float cbx = pk.x - pj.x, cby = pk.y - pj.y, cbz = pk.z - pj.z;
-                    const float cm = sqrtf(cbx * cbx + cby * cby + cbz * cbz) * sqrtf(abx * abx + aby * aby + abz * abz);
-                    float th = 0.f;
-                    if (cm >= 1e-26f)
-                        th = acosf(fminf(1.f, fmaxf(-1.f, (abx * cbx + aby * cby + abz * cbz) / cm)));
-                    const float da = th - kThetaAlpha, db = th - kThetaBeta;
-                    const float term = expf(-kGammaAngle * (kKAlpha * da * da + kEpsAlpha)) +
-                                       expf(-kGammaAngle * (kKBeta * db * db));
-                    ff_add(iacc, -kGammaAngleRecip * logf(term));
-                }
-                // torsions: sum_n V_n (1 + cos(n phi - sigma_n))
-                for (int k = t; k < mol.ntor; k += T) {
-                    const int4 tq = a.tors[mol.tor_off + k];
-                    const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
-                    const float4 p1 = s_ipos[tq.x], p2 = s_ipos[tq.y], p3 = s_ipos[tq.z], p4 = s_ipos[tq.w];
-                    const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
-                    const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
-                    const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
-                    const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
-                    const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
-                    const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
-                    const float phi = atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z),
-                                             c12x * c23x + c12y * c23y + c12z * c23z);
-                    const float e = V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
-                                    V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
-                    ff_add(iacc, e);
-                }
+                bonded_terms(a, mol, s_ipos, L, invL, t, T, iacc);
             }
         }
         __syncthreads();
 
-        // ---- per-molecule partial rows of this CTA's slice
+        // ---- per-molecule partial rows of this CTA's slice (float-float, then double)
         for (int b = warp; b < M; b += NW) {
             FF acc{0.f, 0.f};
-            if (b != mv.m) {
-                const DevMol mb = a.mols[S.mol_off + b];
+            if (b != m) {
+                const DevMol &mb = s_mols[b];
                 const int ob0 = (mb.start < start) ? mb.start : mb.start - n;
                 const int lo = max(ob0, o0), hi = min(ob0 + mb.count, o1);
                 for (int o = lo + lane; o < hi; o += 32) {
@@ -616,10 +717,10 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
                 acc = ff_warp_sum(acc);
             }
             if (lane == 0)
-                s_rowp[b] = (b != mv.m) ? ff_value(acc) : 0.0;
+                s_rowp[b] = (b != m) ? ff_value(acc) : 0.0;
         }
-        {
-            const double v = block_sum_d(ff_value(iacc), s_red);
+        if (flexmol) {
+            const double v = block_sum_ff(iacc, s_red);
             if (t == 0)
                 s_intrap = v;
         }
@@ -639,103 +740,103 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
             }
             if (t == 0) {
                 double v = 0.0;
-                for (int k = 0; k < C; ++k)
-                    v += *cl.map_shared_rank(&s_intrap, k);
+                if (flexmol)
+                    for (int k = 0; k < C; ++k)
+                        v += *cl.map_shared_rank(&s_intrap, k);
                 s_intra_new = v;
             }
+            __syncthreads();
         } else {
-            for (int b = t; b < M; b += T)
-                s_row[b] = s_rowp[b];
             if (t == 0)
-                s_intra_new = s_intrap;
+                s_intra_new = flexmol ? s_intrap : 0.0;
         }
-        __syncthreads();
+        const double *rowv = (C > 1) ? s_row : s_rowp;
         if (warp == 0) {
             double v = 0.0;
             for (int b = lane; b < M; b += 32)
-                if (b != mv.m)
-                    v += s_row[b];
+                if (b != m)
+                    v += rowv[b];
             v = warp_sum_d(v);
             if (lane == 0) {
-                const double new_row = v + (flexmol ? s_intra_new : 0.0);
+                const double new_row = v + s_intra_new;
+                s_new_row = new_row;
                 const double newPotential = s_pot - s_old_row + new_row;
                 const float delta = (float)(newPotential - s_pot);
                 int acc = 0;
                 if (delta < 0.0f) {
                     acc = 1;
                 } else {
-                    const float T_ = a.temperature[g];
-                    const float boltz = expf(-(delta * kKcal) / (kRgas * T_));
-                    acc = (mv.u_metro < (double)boltz) ? 2 : 0;
+                    const float boltz = expf(-(delta * kKcal) / (kRgas * temperature));
+                    acc = ((double)mv.w_metro < (double)boltz * 4294967296.0) ? 2 : 0;
                 }
                 if (!isfinite(newPotential))
                     acc = 0;
                 s_accept = acc;
-                s_pot = acc ? newPotential : s_pot;
+                if (acc)
+                    s_pot = newPotential;
+                if (acc == 1)
+                    st.accept++;
+                else if (acc == 2)
+                    st.acceptA++;
+                else
+                    st.reject++;
+                pairs += (unsigned long long)n * (unsigned long long)(N - n) +
+                         (flexmol ? (unsigned long long)mv.nintra : 0ull);
+                if (nullm)
+                    errbits |= 1u;
             }
         }
         __syncthreads();
 
-        // ---- commit (rank 0 only)
-        if (rank == 0) {
-            const int acc = s_accept;
-            if (acc) {
-                for (int i = t; i < n; i += T) {
-                    float4 p = s_ipos[i];
-                    p.w = 0.f;
-                    a.pos[st0 + start + i] = p;
-                    a.rel[st0 + start + i] = s_irel[i];
-                }
-                for (int b = t; b < M; b += T)
-                    if (b != mv.m) {
-                        E[(long long)mv.m * M + b] = s_row[b];
-                        E[(long long)b * M + mv.m] = s_row[b];
-                    }
-                if (t == 0) {
-                    centers[mv.m] = make_float4(mv.wcx, mv.wcy, mv.wcz, 0.f);
+        // ---- commit
+        const int acc = s_accept;
+        const bool writer = RES || rank == 0;
+        if (acc && writer) {
+            for (int i = t; i < n; i += T) {
+                float4 p = s_ipos[i];
+                p.w = 0.f;
+                P[start + i] = p;
+                Q[start + i] = s_irel[i];
+            }
+            for (int b = t; b < M; b += T) {
+                if (b != m) {
+                    const double nv = rowv[b];
+                    if (RES)
+                        ROWSUM[b] += nv - EM[(long long)m * M + b];
+                    EM[(long long)m * M + b] = nv;
+                    EM[(long long)b * M + m] = nv;
+                } else {
+                    if (RES)
+                        ROWSUM[m] = s_new_row;
                     if (flexmol)
-                        intra[mv.m] = s_intra_new;
-                    a.potential[g] = s_pot;
+                        INTRA[m] = s_intra_new;
                 }
             }
-            if (t == 0) {
-                const DevMol mm = a.mols[S.mol_off + mv.m];
-                a.pairc[g] += (unsigned long long)n * (unsigned long long)(N - n) +
-                              (flexmol ? (unsigned long long)mm.nintra : 0ull);
-                ReplicaStats &stt = a.stats[g];
-                if (acc == 1)
-                    stt.accept++;
-                else if (acc == 2)
-                    stt.acceptA++;
-                else
-                    stt.reject++;
-                if (mv.null_move)
-                    atomicOr(&a.errflags[g], 1u);
-            }
-            // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
-            const int freq = S.sample_freq;
-            if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&
-                (long long)mcstep >= (long long)S.sample_after) {
-                __syncthreads();
-                if (warp == 0) {
-                    double e = 0.0;
-                    if (S.nc_mode == 1) {
-                        const int nc = S.non_crowders;
-                        for (int k = lane; k < nc * nc; k += 32) {
-                            const int aa = k / nc, bb = k % nc;
-                            if (aa < bb)
-                                e += E[(long long)aa * M + bb];
-                        }
-                        e = warp_sum_d(e);
-                    } else if (S.nc_mode == 2) {
-                        e = s_pot;
+            if (t == 0)
+                CEN[m] = make_float4(mv.wcx, mv.wcy, mv.wcz, 0.f);
+        }
+        // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
+        const int freq = S.sample_freq;
+        if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&
+            (long long)mcstep >= (long long)S.sample_after) {
+            __syncthreads();
+            if (warp == 0) {
+                double e = 0.0;
+                if (S.nc_mode == 1) {
+                    const int nc = S.non_crowders;
+                    for (int k = lane; k < nc * nc; k += 32) {
+                        const int aa = k / nc, bb = k % nc;
+                        if (aa < bb)
+                            e += ld_state<RES>(&EM[(long long)aa * M + bb]);
                     }
-                    if (lane == 0) {
-                        ReplicaStats &stt = a.stats[g];
-                        stt.samplesSinceLastExchange++;
-                        if ((float)e < S.bound_threshold)
-                            stt.boundSamples++;
-                    }
+                    e = warp_sum_d(e);
+                } else if (S.nc_mode == 2) {
+                    e = s_pot;
+                }
+                if (lane == 0) {
+                    st.samplesSinceLastExchange++;
+                    if ((float)e < S.bound_threshold)
+                        st.boundSamples++;
                 }
             }
         }
@@ -744,8 +845,30 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
         else
             __syncthreads();
     }
-    if (rank == 0 && t == 0)
-        a.stepc[g] += (unsigned long long)nsteps;
+
+    // ---- write back (rank 0)
+    if (rank == 0) {
+        if (RES) {
+            for (int i = t; i < N; i += T) {
+                gP[i] = P[i];
+                gQ[i] = Q[i];
+            }
+            for (int k = t; k < M; k += T) {
+                gCEN[k] = CEN[k];
+                gINTRA[k] = INTRA[k];
+            }
+            for (int k = t; k < M * M; k += T)
+                gE[k] = EM[k];
+        }
+        if (t == 0) {
+            a.potential[g] = s_pot;
+            a.stats[g] = st;
+            a.stepc[g] = step0 + (unsigned long long)nsteps;
+            a.pairc[g] += pairs;
+            if (errbits)
+                atomicOr(&a.errflags[g], errbits);
+        }
+    }
 }
 
 // ------------------------------------------------------------------ initial energies
@@ -754,15 +877,15 @@ __global__ void __launch_bounds__(256) k_mc_block(EngineArgs a, int nsteps)
 __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double s_red[32];
-    const int t = threadIdx.x, T = blockDim.x, lane = t & 31, warp = t >> 5, NW = T >> 5;
+    __shared__ FF s_red[kMaxWarps];
+    const int t = threadIdx.x, T = blockDim.x;
     const int g = blockIdx.x / a.max_m, am = blockIdx.x % a.max_m;
     const int s = a.rep_sim[g];
     const DevSim S = a.sims[s];
     if (am >= S.M)
         return;
     const int r = g - S.rep_off, N = S.N, M = S.M;
-    const SmemLayout Ly = smem_layout(a.max_mol, a.max_n, a.max_m);
+    const SmemLayout Ly = smem_layout(a.max_mol, a.max_n, a.max_m, a.max_n, 0, a.any_flexible);
     float *s_table = reinterpret_cast<float *>(smem + Ly.table);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
     float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
@@ -803,7 +926,7 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
             }
             ff_add(acc, part);
         }
-        const double v = block_sum_d(ff_value(acc), s_red);
+        const double v = block_sum_ff(acc, s_red);
         if (t == 0) {
             E[(long long)am * M + b] = v;
             E[(long long)b * M + am] = v;
@@ -819,10 +942,7 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
             const int4 ej = s_iexcl[j];
             float part = 0.f;
             for (int i = 0; i < j; ++i) {
-                const int4 ei = s_iexcl[i];
-                const bool ex = (ei.z != 0 && ei.z == ej.z) || (ei.x == ej.x && abs(ei.y - ej.y) < 4) ||
-                                (ei.w != 0 && ei.w == ej.w);
-                if (!ex)
+                if (!intra_excluded(s_iexcl[i], ej))
                     part += pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
                 if ((i & 31) == 31) {
                     ff_add(iacc, part);
@@ -835,49 +955,11 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
             const int2 pr = a.indsub[mol.ind_off + k];
             ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
         }
-        for (int k = t; k < mol.nbond; k += T) {
-            const int2 b = a.bonds[mol.bond_off + k];
-            const float4 pi = s_ipos[b.x], pj = s_ipos[b.y];
-            const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
-                        dz = min_image(pj.z - pi.z, L, invL);
-            const float rr = sqrtf(dx * dx + dy * dy + dz * dz) - kR0;
-            ff_add(iacc, 0.5f * kKSpring * rr * rr);
-        }
-        for (int k = t; k < mol.nang; k += T) {
-            const int4 an = a.angles[mol.ang_off + k];
-            const float4 pi = s_ipos[an.x], pj = s_ipos[an.y], pk = s_ipos[an.z];
-            const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
-            const float cbx = pk.x - pj.x, cby = pk.y - pj.y, cbz = pk.z - pj.z;
-            const float cm = sqrtf(cbx * cbx + cby * cby + cbz * cbz) * sqrtf(abx * abx + aby * aby + abz * abz);
-            float th = 0.f;
-            if (cm >= 1e-26f)
-                th = acosf(fminf(1.f, fmaxf(-1.f, (abx * cbx + aby * cby + abz * cbz) / cm)));
-            const float da = th - kThetaAlpha, db = th - kThetaBeta;
-            const float term =
-                expf(-kGammaAngle * (kKAlpha * da * da + kEpsAlpha)) + expf(-kGammaAngle * (kKBeta * db * db));
-            ff_add(iacc, -kGammaAngleRecip * logf(term));
-        }
-        for (int k = t; k < mol.ntor; k += T) {
-            const int4 tq = a.tors[mol.tor_off + k];
-            const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
-            const float4 p1 = s_ipos[tq.x], p2 = s_ipos[tq.y], p3 = s_ipos[tq.z], p4 = s_ipos[tq.w];
-            const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
-            const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
-            const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
-            const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
-            const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
-            const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
-            const float phi =
-                atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), c12x * c23x + c12y * c23y + c12z * c23z);
-            const float e = V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
-                            V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
-            ff_add(iacc, e);
-        }
+        bonded_terms(a, mol, s_ipos, L, invL, t, T, iacc);
     }
-    const double v = block_sum_d(ff_value(iacc), s_red);
+    const double v = block_sum_ff(iacc, s_red);
     if (t == 0)
         a.intra[S.molst_off + (long long)r * M + am] = (mol.flags & kMolFlexible) ? v : 0.0;
-    (void)lane, (void)warp, (void)NW;
 }
 
 // potential[g] = sum_{a<b} E[a][b] + sum_a intra[a]
@@ -920,8 +1002,8 @@ __device__ void report_slot(ReplicaStats &s, float4 &out)
     out = make_float4(s.fractionBound, s.accumulativeFractionBound, s.acceptanceRatio, s.accumulativeAcceptanceRatio);
 }
 
-// One warp per simulation.  mode bit 0: write the per-temperature report first; bit 1:
-// perform the exchange sweep.  `report_row` selects the report slot.
+// One warp per simulation: the per-temperature report (once sampling has started),
+// then the even/odd exchange sweep.
 __global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block)
 {
     const int s = blockIdx.x;
@@ -1000,34 +1082,31 @@ cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps,
                             cudaStream_t stream)
 {
     const int C = a.cluster;
-    if (C > 1) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(total_replicas * C);
-        cfg.blockDim = dim3(threads);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = C;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, k_mc_block, a, nsteps);
-    }
-    k_mc_block<<<total_replicas, threads, smem, stream>>>(a, nsteps);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(total_replicas * C);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (C > 1) ? 1 : 0;
+    if (a.resident)
+        return cudaLaunchKernelEx(&cfg, k_mc<true>, a, nsteps);
+    return cudaLaunchKernelEx(&cfg, k_mc<false>, a, nsteps);
 }
 
 cudaError_t set_mc_smem_limit(size_t smem)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_mc_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
-    e = cudaFuncSetAttribute(k_init_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
-    return cudaFuncSetAttribute(k_mc_block, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaError_t e = cudaFuncSetAttribute(k_mc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_init_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e;
 }
 
 cudaError_t launch_init_energy(const EngineArgs &a, int total_replicas, size_t smem, double *potential_out,

@@ -41,6 +41,11 @@ struct DevSim {
     float bound_threshold;       // kcal/mol, BOUND_ENERGY_VALUE
     int max_mol;                 // largest molecule
     int pad0;
+    // The same choices as integer thresholds on the raw 32-bit draw w (u = w / 2^32):
+    // u < c  <=>  w < ceil(c * 2^32), so the comparisons are exact without FP64.
+    unsigned long long thr4[4];  // cumulative weights, flexible molecule
+    unsigned long long thr3[3];  // cumulative weights, only molecule
+    unsigned long long thr_rot;  // rigid molecule: rotate below, translate above
 };
 
 struct DevMol {
@@ -108,6 +113,8 @@ struct EngineArgs {
     uint32_t seed_lo, seed_hi;
     int ntypes;
     int cluster;                 // CTAs per replica
+    int resident;                // 1: each CTA keeps its replica's state in shared memory
+    int any_flexible;            // some molecule carries internal energy terms
     int max_n;                   // largest N
     int max_m;                   // largest M
     int max_mol;                 // largest molecule

@@ -44,6 +44,7 @@ _DECL = {
     "cgppd_engine_error_bits": (ctypes.c_uint, [c_void_p]),
     "cgppd_engine_last_launches": (c_int, [c_void_p]),
     "cgppd_engine_launch_shape": (c_int, [c_void_p, P(c_int), P(c_int)]),
+    "cgppd_engine_set_resident": (c_int, [c_void_p, c_int]),
 }
 
 
@@ -134,7 +135,8 @@ class Engine:
             len(segments), _p(seglen, c_int), _p(segres, c_int), _p(c, c_float) if c is not None else None),
             "add_molecule")
 
-    def finalize(self, cluster=0, threads=0):
+    def finalize(self, cluster=0, threads=0, resident=True):
+        _ok(_L().cgppd_engine_set_resident(self.h, int(bool(resident))), "set_resident")
         _ok(_L().cgppd_engine_finalize(self.h, int(cluster), int(threads)), "finalize")
 
     def run(self, n_blocks, steps_per_block, exchange_after_last=True, stream=None):
@@ -229,12 +231,14 @@ class Engine:
         return _L().cgppd_engine_last_launches(self.h)
 
     def launch_shape(self):
+        """(CTAs per replica, threads per CTA, state resident in shared memory)."""
         c, t = c_int(), c_int()
-        _L().cgppd_engine_launch_shape(self.h, ctypes.byref(c), ctypes.byref(t))
-        return c.value, t.value
+        res = _L().cgppd_engine_launch_shape(self.h, ctypes.byref(c), ctypes.byref(t))
+        return c.value, t.value, bool(res)
 
 
-def from_workload(wl, cluster=0, threads=0, seed=None, sample_frequency=0, sample_after=0, finalize=True):
+def from_workload(wl, cluster=0, threads=0, seed=None, sample_frequency=0, sample_after=0, finalize=True,
+                  resident=True):
     """Engine holding every simulation of a workloads.Workload."""
     e = Engine(wl.lj_raw, wl.torsion_V, wl.torsion_phase, seed=wl.seed if seed is None else seed)
     for sim in wl.sims:
@@ -245,5 +249,5 @@ def from_workload(wl, cluster=0, threads=0, seed=None, sample_frequency=0, sampl
                            chain_index=m.chain_index, all_flexible=m.all_flexible, crowder=m.crowder,
                            segments=m.segments)
     if finalize:
-        e.finalize(cluster, threads)
+        e.finalize(cluster, threads, resident)
     return e

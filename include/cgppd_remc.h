@@ -136,8 +136,13 @@ unsigned cgppd_engine_error_bits(cgppd_engine *e);
 /* Kernel launches enqueued by the last cgppd_engine_run call. */
 int cgppd_engine_last_launches(const cgppd_engine *e);
 
-/* Launch shape in use: CTAs per replica and threads per CTA. */
+/* Launch shape in use: CTAs per replica and threads per CTA; returns 1 when each
+ * CTA keeps its replica's state in shared memory for the whole launch, else 0. */
 int cgppd_engine_launch_shape(const cgppd_engine *e, int *cluster, int *threads);
+
+/* Before finalize: allow (1, default) or forbid (0) shared-memory-resident replica
+ * state; it is used only when the state fits. */
+int cgppd_engine_set_resident(cgppd_engine *e, int allow);
 
 #ifdef __cplusplus
 }

@@ -37,10 +37,10 @@ def subset(wl, nrep):
                                 sim.rotate_steps[:nrep], sim.move_weights, sim.rigid_rotate_prob)
 
 
-def engine_for(wl, sims, cluster=1, threads=256, sample_frequency=0, sample_after=0):
+def engine_for(wl, sims, cluster=1, threads=256, sample_frequency=0, sample_after=0, resident=True):
     w2 = workloads.Workload(wl.name, sims, wl.lj_raw, wl.torsion_V, wl.torsion_phase, wl.seed)
     return eng.from_workload(w2, cluster=cluster, threads=threads, sample_frequency=sample_frequency,
-                             sample_after=sample_after)
+                             sample_after=sample_after, resident=resident)
 
 
 def oracle_for(wl, sim, mode=oracle.REF, **kw):
@@ -117,11 +117,13 @@ def compare_runs(e, o, sim_index=0, pos_tol=2e-3, traj_rel=REL):
         assert abs(rep["potential"][r] - e64) <= REL * abs(e64) + 1e-9, (r, rep["potential"][r], e64)
 
 
+@pytest.mark.parametrize("resident", [True, False])
 @pytest.mark.parametrize("config,nrep,blocks,steps", [("c0", 4, 3, 100), ("c4", 4, 2, 60), ("c1", 4, 3, 100)])
-def test_trajectory_matches_oracle(config, nrep, blocks, steps):
+def test_trajectory_matches_oracle(config, nrep, blocks, steps, resident):
     wl = workloads.make(config)
     sim = subset(wl, nrep)
-    e = engine_for(wl, [sim])
+    e = engine_for(wl, [sim], resident=resident)
+    assert e.launch_shape()[2] == resident
     o = oracle_for(wl, sim)
     e.run(blocks, steps, exchange_after_last=True)
     orep, oex = o.run(blocks, steps, exchange_after_last=True)
@@ -134,12 +136,13 @@ def test_trajectory_matches_oracle(config, nrep, blocks, steps):
         assert tuple(ex) == tuple(oex[b])
 
 
+@pytest.mark.parametrize("resident", [True, False])
 @pytest.mark.parametrize("cluster", [2, 4])
-def test_cluster_split_matches_single_cta(cluster):
+def test_cluster_split_matches_single_cta(cluster, resident):
     wl = workloads.make("c4")
     sim = subset(wl, 3)
-    e1 = engine_for(wl, [sim], cluster=1)
-    ec = engine_for(wl, [sim], cluster=cluster)
+    e1 = engine_for(wl, [sim], cluster=1, resident=resident)
+    ec = engine_for(wl, [sim], cluster=cluster, resident=resident)
     assert ec.launch_shape()[0] == cluster
     e1.run(2, 80)
     ec.run(2, 80)
@@ -165,6 +168,18 @@ def test_running_total_has_no_drift():
         xyz, _, _ = e.state(0, r)
         ref = np.triu(oracle_matrix(wl, sim, xyz), 1).sum()
         assert abs(run_tot[r] - ref) <= REL * abs(ref) + 1e-9
+
+
+@pytest.mark.parametrize("config", ["c1", "c4"])
+def test_flexible_and_rigid_clusters_match_oracle(config):
+    # flexible moves and crankshafts split over a cluster, state resident
+    wl = workloads.make(config)
+    sim = subset(wl, 3)
+    e = engine_for(wl, [sim], cluster=2)
+    o = oracle_for(wl, sim)
+    e.run(2, 80)
+    o.run(2, 80)
+    compare_runs(e, o, traj_rel=REL if config != "c1" else 2e-4)
 
 
 def test_batched_simulations_match_separate_oracles():
