@@ -216,20 +216,20 @@ __device__ __forceinline__ bool intra_excluded(int4 ei, int4 ej)
     return (ei.z != 0 && ei.z == ej.z) || (ei.x == ej.x && abs(ei.y - ej.y) < 4) || (ei.w != 0 && ei.w == ej.w);
 }
 
-// Bonded terms of one molecule at coordinates `p` (kcal/mol), thread-strided from
-// `t0` with stride `stride` (src/Potential.cpp:45-98 with Potential::total's factors).
-__device__ void bonded_terms(const EngineArgs &a, const DevMol &mol, const float4 *p, float L, float invL, int t0,
-                             int stride, FF &acc)
+// One bonded term (kcal/mol) of a molecule at coordinates `p`: kind 0 bond, 1 angle,
+// 2 torsion (src/Potential.cpp:45-98 with Potential::total's factors).
+__device__ float bonded_item(const EngineArgs &a, const DevMol &mol, const float4 *p, float L, float invL, int kind,
+                             int k)
 {
-    for (int k = t0; k < mol.nbond; k += stride) {
+    if (kind == 0) {  // 0.5 K (r - R0)^2, minimum-image distance
         const int2 b = a.bonds[mol.bond_off + k];
         const float4 pi = p[b.x], pj = p[b.y];
         const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
                     dz = min_image(pj.z - pi.z, L, invL);
         const float rr = sqrtf(dx * dx + dy * dy + dz * dz) - kR0;
-        ff_add(acc, 0.5f * kKSpring * rr * rr);
+        return 0.5f * kKSpring * rr * rr;
     }
-    for (int k = t0; k < mol.nang; k += stride) {
+    if (kind == 1) {  // -(1/gamma) log(exp(-gamma(ka(t-ta)^2 + ea)) + exp(-gamma kb (t-tb)^2))
         const int4 an = a.angles[mol.ang_off + k];
         const float4 pi = p[an.x], pj = p[an.y], pk = p[an.z];
         const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
@@ -241,23 +241,33 @@ __device__ void bonded_terms(const EngineArgs &a, const DevMol &mol, const float
         const float da = th - kThetaAlpha, db = th - kThetaBeta;
         const float term =
             expf(-kGammaAngle * (kKAlpha * da * da + kEpsAlpha)) + expf(-kGammaAngle * (kKBeta * db * db));
-        ff_add(acc, -kGammaAngleRecip * logf(term));
+        return -kGammaAngleRecip * logf(term);
     }
-    for (int k = t0; k < mol.ntor; k += stride) {
-        const int4 tq = a.tors[mol.tor_off + k];
-        const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
-        const float4 p1 = p[tq.x], p2 = p[tq.y], p3 = p[tq.z], p4 = p[tq.w];
-        const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
-        const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
-        const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
-        const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
-        const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
-        const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
-        const float phi =
-            atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), c12x * c23x + c12y * c23y + c12z * c23z);
-        const float e = V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
-                        V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
-        ff_add(acc, e);
+    // sum_n V_n (1 + cos(n phi - sigma_n))
+    const int4 tq = a.tors[mol.tor_off + k];
+    const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
+    const float4 p1 = p[tq.x], p2 = p[tq.y], p3 = p[tq.z], p4 = p[tq.w];
+    const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
+    const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
+    const float b3x = p4.x - p3.x, b3y = p4.y - p3.y, b3z = p4.z - p3.z;
+    const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
+    const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
+    const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
+    const float phi = atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), c12x * c23x + c12y * c23y + c12z * c23z);
+    return V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
+           V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
+}
+
+// Bonded terms of one molecule, one flat index over bonds, angles and torsions so that
+// each thread evaluates one term: thread-strided from t0 by `stride`.
+__device__ void bonded_terms(const EngineArgs &a, const DevMol &mol, const float4 *p, float L, float invL, int t0,
+                             int stride, FF &acc)
+{
+    const int nb = mol.nbond, na = mol.nang, nt = mol.ntor;
+    for (int k = t0; k < nb + na + nt; k += stride) {
+        const int kind = (k < nb) ? 0 : (k < nb + na) ? 1 : 2;
+        const int kk = (kind == 0) ? k : (kind == 1) ? k - nb : k - nb - na;
+        ff_add(acc, bonded_item(a, mol, p, L, invL, kind, kk));
     }
 }
 
@@ -1101,6 +1111,12 @@ cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps,
 
 cudaError_t set_mc_smem_limit(size_t smem)
 {
+    // The attribute belongs to the kernel, not to an engine: never lower it below what an
+    // engine created earlier (and its captured graphs) needs.
+    static size_t s_max = 0;
+    if (smem <= s_max)
+        return cudaSuccess;
+    s_max = smem;
     cudaError_t e = cudaFuncSetAttribute(k_mc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
