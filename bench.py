@@ -301,6 +301,7 @@ def gpu_arm(args):
                        "threads_per_cta": shape[1], "state_in_shared_memory": shape[2], "parallelism": "replicas on one GPU" if world == 1 else
                        "dp%d (independent replica sets)" % world},
             "pair_evals_per_s": pair_rate,
+            "autotune_us_per_mc_step": [list(x) for x in e.tuning()],
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved / peak_tflops, "traffic": traffic,
                          "kernel": "k_mc_block", "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,

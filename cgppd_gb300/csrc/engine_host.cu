@@ -139,6 +139,12 @@ struct cgppd_engine {
     std::vector<DevSim> h_sims;
     std::vector<DevMol> h_mols;
 
+    struct TuneResult {
+        int cluster, threads;
+        float us_per_step;
+    };
+    std::vector<TuneResult> tuning;  // the autotuner's measurements (empty if not run)
+
     ~cgppd_engine()
     {
         for (auto &kv : graphs)
@@ -466,6 +472,103 @@ int cgppd_engine::build()
     return rc ? -1 : 0;
 }
 
+// ------------------------------------------------------------------ launch shape
+
+// CTAs per replica C and threads per CTA T; the state is kept in shared memory when the
+// per-CTA footprint stays under 160 KB.
+static void configure_shape(cgppd_engine *e, int C, int T)
+{
+    e->cluster = C;
+    e->threads = T;
+    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible);
+    e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024;
+    e->smem = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, e->resident, e->any_flexible);
+}
+
+// Autotuner: time k_mc for each candidate launch shape on scratch copies of the mutable
+// state (the real trajectory is not advanced) and keep the fastest.  Results are cached
+// per system shape for the life of the process.
+static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
+{
+    static std::map<std::vector<long long>, std::pair<int, int>> cache;
+    std::vector<long long> key{e->total_replicas, e->max_n, e->max_m, e->max_mol, e->any_flexible, e->resident_pref,
+                               fixed_cluster, fixed_threads};
+    for (const auto &s : e->h_sims)
+        key.push_back(((long long)s.N << 32) | ((long long)s.M << 16) | s.R);
+    auto hit = cache.find(key);
+    if (hit != cache.end()) {
+        configure_shape(e, hit->second.first, hit->second.second);
+        return 0;
+    }
+    DevBuf<float4> pos, rel, cen;
+    DevBuf<double> em, in, pot;
+    DevBuf<ReplicaStats> st;
+    DevBuf<unsigned long long> sc, pc;
+    DevBuf<unsigned> ef;
+    auto clone = [](auto &dst, const auto &src) {
+        if (dst.alloc(src.n) != 0)
+            return -1;
+        return cgppd_check(cudaMemcpy(dst.ptr, src.ptr, src.n * sizeof(*src.ptr), cudaMemcpyDeviceToDevice),
+                           "autotune copy");
+    };
+    if (clone(pos, e->d_pos) || clone(rel, e->d_rel) || clone(cen, e->d_center) || clone(em, e->d_emat) ||
+        clone(in, e->d_intra) || clone(pot, e->d_potential) || clone(st, e->d_stats) || clone(sc, e->d_stepc) ||
+        clone(pc, e->d_pairc) || clone(ef, e->d_errflags))
+        return -1;
+    EngineArgs base = e->args();
+    base.pos = pos.ptr, base.rel = rel.ptr, base.center = cen.ptr, base.emat = em.ptr, base.intra = in.ptr;
+    base.potential = pot.ptr, base.stats = st.ptr, base.stepc = sc.ptr, base.pairc = pc.ptr, base.errflags = ef.ptr;
+    const int clusters[4] = {1, 2, 4, 8}, thread_opts[2] = {128, 256};
+    const int steps = 32;
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    float best = 1e30f;
+    int bc = 1, bt = 256;
+    e->tuning.clear();
+    for (int C : clusters) {
+        if (fixed_cluster > 0 && C != fixed_cluster)
+            continue;
+        for (int T : thread_opts) {
+            if (fixed_threads > 0 && T != fixed_threads)
+                continue;
+            configure_shape(e, C, T);
+            if (e->smem > 227 * 1024 || set_mc_smem_limit(e->smem) != cudaSuccess)
+                continue;
+            EngineArgs a = base;
+            a.cluster = C;
+            a.resident = e->resident;
+            if (launch_mc_block(a, e->total_replicas, 4, T, e->smem, e->own_stream) != cudaSuccess) {
+                cudaGetLastError();  // a shape the device cannot schedule: skip it
+                continue;
+            }
+            cudaEventRecord(ev0, e->own_stream);
+            cudaError_t err = launch_mc_block(a, e->total_replicas, steps, T, e->smem, e->own_stream);
+            cudaEventRecord(ev1, e->own_stream);
+            if (err != cudaSuccess || cudaEventSynchronize(ev1) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev0, ev1);
+            const float us = 1000.f * ms / steps;
+            e->tuning.push_back({C, T, us});
+            if (us < best * 0.97f) {  // prefer the smaller shape unless clearly faster
+                best = us;
+                bc = C;
+                bt = T;
+            }
+        }
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "autotune") != 0)
+        return -1;
+    configure_shape(e, bc, bt);
+    cache[key] = std::make_pair(bc, bt);
+    return 0;
+}
+
 // ------------------------------------------------------------------ C ABI
 
 extern "C" {
@@ -570,26 +673,12 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
         return cgppd_fail("cgppd_engine_finalize: no simulation");
     if (e->build() != 0)
         return -1;
-    e->threads = (threads == 128) ? 128 : 256;
-    if (cluster <= 0) {
-        // enough CTAs to cover the SMs at least once when replicas are few
-        int dev = 0, sms = 152;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cluster = 1;
-        while (cluster < 8 && e->total_replicas * cluster < sms && e->max_n / (cluster * 2) >= e->threads / 4)
-            cluster *= 2;
-    }
-    e->cluster = std::min(8, std::max(1, cluster));
-    // keep each replica's state in shared memory when it fits (<= 160 KB per CTA)
-    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, e->cluster, 1, e->any_flexible);
-    e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024;
-    const size_t s_mc = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, e->cluster, e->resident, e->any_flexible);
+    const bool tune = cluster <= 0 || threads <= 0;
+    configure_shape(e, std::min(8, std::max(1, cluster > 0 ? cluster : 1)), threads == 128 ? 128 : 256);
     const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
-    e->smem = s_mc;
-    if (std::max(s_mc, s_init) > 227 * 1024)
+    if (std::max(e->smem, s_init) > 227 * 1024)
         return cgppd_fail("cgppd_engine_finalize: system too large for shared memory (reduce molecule size or N)");
-    if (cgppd_check(set_mc_smem_limit(std::max(s_mc, s_init)), "engine shared-memory limit") != 0)
+    if (cgppd_check(set_mc_smem_limit(std::max(e->smem, s_init)), "engine shared-memory limit") != 0)
         return -1;
     if (cgppd_check(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking), "engine stream") != 0)
         return -1;
@@ -599,7 +688,21 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
         return -1;
     if (cgppd_check(cudaStreamSynchronize(e->own_stream), "initial energy") != 0)
         return -1;
+    if (tune && autotune(e, cluster, threads) != 0)
+        return -1;
     e->finalized = true;
+    return 0;
+}
+
+int cgppd_engine_tuning(const cgppd_engine *e, int *n, int *clusters, int *threads, float *us_per_step)
+{
+    const int k = (int)e->tuning.size();
+    for (int i = 0; i < k && i < *n; ++i) {
+        clusters[i] = e->tuning[i].cluster;
+        threads[i] = e->tuning[i].threads;
+        us_per_step[i] = e->tuning[i].us_per_step;
+    }
+    *n = k;
     return 0;
 }
 

@@ -251,3 +251,21 @@ def from_workload(wl, cluster=0, threads=0, seed=None, sample_frequency=0, sampl
     if finalize:
         e.finalize(cluster, threads, resident)
     return e
+
+
+def _tuning(self):
+    """Autotuner measurements: list of (CTAs per replica, threads per CTA, us per MC step)."""
+    L = _L()
+    if not hasattr(L, "_tuning_declared"):
+        L.cgppd_engine_tuning.restype = c_int
+        L.cgppd_engine_tuning.argtypes = [c_void_p, P(c_int), P(c_int), P(c_int), P(c_float)]
+        L._tuning_declared = True
+    n = c_int(16)
+    cl = (c_int * 16)()
+    th = (c_int * 16)()
+    us = (c_float * 16)()
+    L.cgppd_engine_tuning(self.h, ctypes.byref(n), cl, th, us)
+    return [(cl[i], th[i], us[i]) for i in range(n.value)]
+
+
+Engine.tuning = _tuning

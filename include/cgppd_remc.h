@@ -67,9 +67,14 @@ int cgppd_engine_add_molecule(cgppd_engine *e, int sim, int n, const float *xyz,
 
 /* Build the device tables, upload every replica and compute the initial energies
  * (Simulation::init: initialReplica.E() + internal_molecule_E(true), replicated to
- * every replica).  cluster: CTAs per replica (1..8, 0 = automatic); threads: 128 or
- * 256 (0 = 256). */
+ * every replica).  cluster: CTAs per replica (1, 2, 4, 8); threads per CTA (128, 256);
+ * 0 for either lets the autotuner pick it from a timed sweep on scratch copies of the
+ * state (cached per system shape for the life of the process). */
 int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads);
+
+/* The autotuner's measurements: on input *n is the capacity of the arrays, on output
+ * the number of shapes timed (0 if the shape was given). */
+int cgppd_engine_tuning(const cgppd_engine *e, int *n, int *clusters, int *threads, float *us_per_step);
 
 /* Replaces MCthreadableFunction's MC loop and Simulation::run's exchange loop
  * (src/Simulation.cpp:737-816, :1044-1092): n_blocks blocks of steps_per_block MC
