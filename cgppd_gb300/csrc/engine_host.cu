@@ -1067,3 +1067,32 @@ int cgppd_engine_launch_shape(const cgppd_engine *e, int *cluster, int *threads)
 }
 
 }  // extern "C"
+
+extern "C" int cgppd_graph_counts(int n, const char *chain_ids, int all_flexible, int n_segments,
+                                  const int *seg_lengths, const int *seg_residues, int num_chains, int *counts9)
+{
+    if (n <= 0)
+        return cgppd_fail("cgppd_graph_counts: empty molecule");
+    std::vector<char> chains(chain_ids, chain_ids + n);
+    std::vector<std::vector<int>> segs;
+    int off = 0;
+    for (int k = 0; k < n_segments; ++k) {
+        segs.emplace_back(seg_residues + off, seg_residues + off + seg_lengths[k]);
+        for (int v : segs.back())
+            if (v < 0 || v >= n)
+                return cgppd_fail("cgppd_graph_counts: segment residue out of range");
+        off += seg_lengths[k];
+    }
+    Graph g;
+    g.init(chains, all_flexible != 0, segs, num_chains);
+    counts9[0] = (int)g.bonds.size();
+    counts9[1] = (int)g.angles.size();
+    counts9[2] = (int)g.torsions.size();
+    counts9[3] = (int)g.rigid_domains.size();
+    counts9[4] = (int)g.segment_bonds.size();
+    counts9[5] = (int)g.indirect_neighbours.size();
+    counts9[6] = (int)g.MC_local_residues.size();
+    counts9[7] = (int)g.MC_crankshaft_residues.size();
+    counts9[8] = (int)g.MC_flex_residues.size();
+    return 0;
+}

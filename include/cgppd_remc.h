@@ -149,6 +149,13 @@ int cgppd_engine_launch_shape(const cgppd_engine *e, int *cluster, int *threads)
  * state; it is used only when the state fits. */
 int cgppd_engine_set_resident(cgppd_engine *e, int allow);
 
+/* Replaces Graph::init for inspection (src/Geometry.cpp:34-192): the flexible-segment
+ * graph of one molecule of n residues.  counts9 = {bonds, angles, torsions, rigid
+ * domains, segment bonds, indirect neighbours, local residues, crankshaft residues,
+ * flex residues}. */
+int cgppd_graph_counts(int n, const char *chain_ids, int all_flexible, int n_segments, const int *seg_lengths,
+                       const int *seg_residues, int num_chains, int *counts9);
+
 #ifdef __cplusplus
 }
 #endif

@@ -338,10 +338,10 @@ void oracle_E_intra(int mode, int n, const float *xyz, const int *aa, const floa
         int r1 = aa[tt[1]], r2 = aa[tt[2]];
         const double *V = torsV + 4 * (r1 * ntypes_t + r2), *S = torsS + 4 * (r1 * ntypes_t + r2);
         double pot = 0.0;
-        for (int k = 0; k < 4; k++) {
-            double nphi = (mode == ORACLE_REF) ? (double)((float)(k + 1) * (float)phi) : (k + 1) * phi;
-            pot += (1.0 + cos(nphi - S[k])) * V[k];
-        }
+        /* phi holds atan2f's float result in a double variable, so n * phi is a double
+         * product in both modes (src/Potential.cpp:84-93) */
+        for (int k = 0; k < 4; k++)
+            pot += (1.0 + cos((k + 1) * phi - S[k])) * V[k];
         T += pot;
     }
     out[0] = LJ;
