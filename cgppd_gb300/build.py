@@ -31,9 +31,12 @@ def cuda_home():
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build cgppd_gb300")
 
 
+APP = os.path.join(LIBDIR, "cgppd")
+
+
 def _sources():
-    cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*", "*.cu")))
-    cpp = sorted(glob.glob(os.path.join(CSRC, "*.cpp")) + glob.glob(os.path.join(CSRC, "*", "*.cpp")))
+    cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "host", "*.cu")))
+    cpp = sorted(glob.glob(os.path.join(CSRC, "*.cpp")) + glob.glob(os.path.join(CSRC, "host", "*.cpp")))
     return cu, cpp
 
 
@@ -92,6 +95,10 @@ def build(verbose=False, ptxas_info=False):
             outs = list(ex.map(_run, jobs))
     if jobs or not os.path.exists(LIB):
         _run([nvcc, GENCODE, "-shared", "-o", LIB] + objs + ["-lpthread"])
+    # the `cgppd` command, linked against the library (found next to it at run time)
+    app_src = os.path.join(CSRC, "app", "cgppd_main.cpp")
+    if not os.path.exists(APP) or os.path.getmtime(APP) < max(os.path.getmtime(LIB), os.path.getmtime(app_src)):
+        _run(["g++", "-O2", "-o", APP, app_src, "-L" + LIBDIR, "-lcgppd_gb300", "-Wl,-rpath,$ORIGIN"])
     if verbose or ptxas_info:
         for o in outs:
             if o.strip():

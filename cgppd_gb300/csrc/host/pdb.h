@@ -1,0 +1,44 @@
+// pdb.h -- C-alpha records of a PDB file and the placement of a molecule.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "amino_acids.h"
+
+namespace cgppd {
+
+struct PdbResidue {
+    std::string name;  // residue name
+    char chain;        // chain identifier (column 22)
+    int res_seq;       // residue sequence number
+    int chain_index;   // number of TER records before this residue
+    int type;          // residue-type index, -1 if the name is unknown
+    float x, y, z;
+};
+
+// Molecule::initFromPDB (src/Molecule.cpp:506-612): ATOM records whose atom name is CA,
+// TER counts chains, a record starting with END stops reading, a file with residues but
+// no TER has one chain.  Throws a const char* when the file cannot be opened or holds an
+// unknown residue name (the reference would index its tables with -1).
+std::vector<PdbResidue> read_pdb(const std::string &path, const AminoAcids &aa, int *num_chains);
+
+// A molecule as Molecule::init leaves it: centre = float mean of the file's positions,
+// relative positions, then `p(x,y,z)` (set the centre) or `t(x,y,z)` (translate and
+// wrap the centre), then a rotation about the normalised axis by `angle` rad
+// (src/Molecule.cpp:25-64, :183-208).
+struct PlacedMolecule {
+    std::vector<PdbResidue> residues;
+    int num_chains = 1;
+    std::vector<float> pos, rel;  // 3n each
+    float center[3] = {0, 0, 0};
+};
+
+PlacedMolecule place_molecule(const std::vector<PdbResidue> &res, int num_chains, bool translate, float px, float py,
+                              float pz, float rx, float ry, float rz, float angle, float box);
+
+// Reference PDB output of one molecule's C-alpha trace (src/Replica.cpp:1124-1168 format).
+void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float *pos, const AminoAcids &aa,
+                     int *atom_counter);
+
+}  // namespace cgppd

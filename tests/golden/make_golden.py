@@ -206,6 +206,34 @@ KATS = {
 }
 
 
+def remc_outputs(ref, arch):
+    """Statistics of the reference's seeded REMC regression output
+    (tests/remctest_<arch>.tgz, checked by tests/testSimulation.cpp:97-150)."""
+    import tarfile
+    out = {}
+    with tarfile.open(os.path.join(ref, "tests", "remctest_%s.tgz" % arch)) as tf:
+        def text(name):
+            return tf.extractfile("remctest_%s/%s" % (arch, name)).read().decode()
+        acc = text("acceptance_ratios").splitlines()
+        out["acceptance_header"] = acc[:2]
+        rows = [ln for ln in acc[2:] if ":" in ln]
+        vals = [[float(x) for x in ln.split(":", 1)[1].replace("|", " ").split()] for ln in rows]
+        out["acceptance_rows"] = len(rows)
+        out["acceptance_final_cumulative"] = vals[-1][1::2]
+        out["acceptance_mean_instantaneous"] = [sum(v[2 * t] for v in vals) / len(vals) for t in range(5)]
+        ex = [ln.split() for ln in text("exchange_freq").splitlines()[1:]]
+        out["exchange_rows"] = len(ex)
+        out["exchange_final_cumulative"] = float(ex[-1][1])
+        fb = text("fractionBound").splitlines()
+        out["fraction_header"] = fb[:3]
+        frows = [ln for ln in fb[3:] if ":" in ln]
+        fvals = [[float(x) for x in ln.split(":", 1)[1].replace("|", " ").split()] for ln in frows]
+        out["fraction_final_cumulative"] = fvals[-1][1::2]
+        out["fileindex"] = text("fileindex").splitlines()
+        out["boundconformations_header"] = text("boundconformations").splitlines()[:2]
+    return out
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     recs = parse_amino_acids(os.path.join(ref, "data/AminoAcids"))
@@ -219,8 +247,19 @@ def main():
         pdbs["tests/" + name] = parse_pdb(os.path.join(ref, "tests/%s.pdb" % name), recs)
     for name in ("ubq", "uim"):
         pdbs["application/" + name] = parse_pdb(os.path.join(ref, "data/application/%s.pdb" % name), recs)
+    with open(os.path.join(ref, "data", "torsional_pair_potentials")) as f:
+        torsion_text = f.read()
+    with open(os.path.join(ref, "tests", "argtestfile")) as f:
+        argtestfile = f.read()
+    with open(os.path.join(ref, "tests", "remctestfile")) as f:
+        remctestfile = f.read()
     out = {"amino_acids": recs, "lj_table": lj, "torsion_V": V, "torsion_sigma": S,
            "pdbs": pdbs, "kats": KATS,
+           # the reference's own test inputs (tests/argtestfile, tests/remctestfile) and the
+           # statistics of its seeded REMC outputs, CPU and GPU builds
+           "argtestfile": argtestfile, "remctestfile": remctestfile,
+           "remctest": {"CPU": remc_outputs(ref, "CPU"), "GPU": remc_outputs(ref, "GPU")},
+           "torsion_file_lines": len(torsion_text.splitlines()),
            "source": "CGPPD reference data/ and tests/ (see make_golden.py)"}
     path = os.path.join(HERE, "reference_data.json")
     with open(path, "w") as f:

@@ -31,6 +31,45 @@ def write_lj_file(path, recs, table):
             f.write("%s %s\n" % (LJ_LABELS[k], vals))
 
 
+def write_torsion_file(path, recs, V, S):
+    """Torsion table in the reference's `NAME NAME V N SIGMA(deg)` format."""
+    with open(path, "w") as f:
+        f.write("# NAME NAME V N SIGMA\n")
+        for i in range(20):
+            for j in range(20):
+                for n in range(4):
+                    if V[i][j][n] != 0.0 or S[i][j][n] != 0.0:
+                        f.write("%s %s %12.6f %d %12.6f\n" % (recs[i]["sname"].upper(), recs[j]["sname"].upper(),
+                                                               V[i][j][n], n + 1, S[i][j][n] * 57.29577951308232))
+
+
+def write_pdb(path, residues):
+    """C-alpha records in fixed PDB columns (what Molecule::initFromPDB reads)."""
+    with open(path, "w") as f:
+        chain = None
+        for k, r in enumerate(residues):
+            if chain is not None and r["chain_index"] != chain:
+                f.write("TER\n")
+            chain = r["chain_index"]
+            x, y, z = r["xyz"]
+            f.write("ATOM  %5d  CA  %3s %c%4d    %8.3f%8.3f%8.3f  1.00  0.00\n" % (k + 1, r["res"], r["chain"],
+                                                                                r["seq"], x, y, z))
+        f.write("TER\nEND\n")
+
+
+def write_reference_data_dir(root, refdata):
+    """data/AminoAcids, data/pair_potentials_MJ1996, data/torsional_pair_potentials and
+    data/application/{ubq,uim}.pdb under `root`, from the fixtures."""
+    d = os.path.join(root, "data")
+    os.makedirs(os.path.join(d, "application"), exist_ok=True)
+    write_amino_acid_file(os.path.join(d, "AminoAcids"), refdata["amino_acids"])
+    write_lj_file(os.path.join(d, "pair_potentials_MJ1996"), refdata["amino_acids"], refdata["lj_table"])
+    write_torsion_file(os.path.join(d, "torsional_pair_potentials"), refdata["amino_acids"], refdata["torsion_V"],
+                       refdata["torsion_sigma"])
+    for name in ("ubq", "uim"):
+        write_pdb(os.path.join(d, "application", name + ".pdb"), refdata["pdbs"]["application/" + name]["residues"])
+
+
 def header_functions():
     """Function names declared in include/*.h."""
     names = []

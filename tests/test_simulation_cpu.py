@@ -1,0 +1,87 @@
+"""Argfile and command-line parsing of the C++ Simulation (no GPU).
+
+Reproduces the reference's tests/testSimulation.cpp:7-94 on the same inputs: the
+argtestfile and command line of that test (the file's text is in the fixtures).
+"""
+import ctypes
+
+import pytest
+
+import cgppd_gb300
+
+
+def dump(argv, mode, cwd):
+    L = cgppd_gb300.lib()
+    f = L.cgppd_args_dump
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+    arr = (ctypes.c_char_p * (len(argv) + 1))(*[a.encode() for a in argv], None)
+    buf = ctypes.create_string_buffer(1 << 16)
+    import os
+    old = os.getcwd()
+    os.chdir(cwd)
+    try:
+        rc = f(len(argv), arr, mode, buf, len(buf))
+    finally:
+        os.chdir(old)
+    text = buf.value.decode()
+    if rc != 0:
+        return rc, text
+    return rc, dict(ln.split("=", 1) for ln in text.splitlines() if "=" in ln)
+
+
+@pytest.fixture()
+def argdir(tmp_path, refdata):
+    (tmp_path / "tests").mkdir()
+    (tmp_path / "tests" / "argtestfile").write_text(refdata["argtestfile"])
+    return tmp_path
+
+
+def test_command_line(argdir):
+    # tests/testSimulation.cpp:8-44
+    argv = ["my_programname", "-f", "tests/argtestfile", "-p", "-q", "-t", "23", "-s", "23", "-g", "23", "-z", "2",
+            "-m", "23", "-e", "23", "-r", "23", "-b", "23", "-n", "23", "-x", "23", "-d", "23"]
+    rc, p = dump(argv, 1 | 4, argdir)
+    assert rc == 0, p
+    assert p["viewConditions"] == "0" and p["skipsimulation"] == "1"
+    assert p["cuda_blockSize"] == "23" and p["auto_blockdim"] == "0"
+    for k in ("threads", "streams", "gpus", "MCsteps", "REsteps", "replicas"):
+        assert p[k] == "23", k
+    assert p["gpuoffset"] == "2"
+    assert p["sampleFrequency"] == "5000" and p["sampleStartsAfter"] == "5000"
+    assert p["inputFile"] == "1" and p["nonCrowders"] == "0" and p["pid"] == "0" and p["resume"] == "0"
+    assert float(p["bound"]) == 23.0 and float(p["temperatureMin"]) == 23.0 and float(p["temperatureMax"]) == 23.0
+    assert p["prefix"] == "" and p["file"] == "tests/argtestfile"
+
+
+def test_config_file(argdir):
+    # tests/testSimulation.cpp:46-94
+    rc, p = dump(["x", "tests/argtestfile"], 2 | 8, argdir)
+    assert rc == 0, p
+    assert p["skipsimulation"] == "0" and p["auto_blockdim"] == "1"
+    assert p["threads"] == "1" and p["streams"] == "1" and p["gpus"] == "1"
+    assert p["MCsteps"] == "10000" and p["REsteps"] == "10000" and p["replicas"] == "1"
+    assert p["sampleFrequency"] == "1000" and p["sampleStartsAfter"] == "1000"
+    assert p["nonCrowders"] == "2"
+    assert float(p["bound"]) == 100.0 and float(p["temperatureMin"]) == 288.0 and float(p["temperatureMax"]) == 300.0
+    assert p["prefix"] == "" and p["title"] == "Config file for unit tests"
+    assert p["molecules"] == "7" and p["named"] == "2"
+    mols = [p["mol%d" % i].split() for i in range(7)]
+    ubq, uim = mols[0], mols[1]
+    assert ubq[1] == "ubiquitin" and uim[1] == "UIM1"
+    assert uim[11] == "1" and uim[12] == "0"           # UIM1 all flexible, no segments
+    assert ubq[11] == "0" and ubq[12] == "1" and ubq[13] == "[72,73,74,75]"
+    assert [m[10] for m in mols] == ["0", "0", "1", "1", "1", "1", "1"]   # crowders
+    assert ubq[2] == "0" and mols[2][2] == "1"          # p(...) sets, t(...) translates
+    assert [float(v) for v in ubq[3:10]] == [45.0, 45.0, 45.0, 0.0, 1.0, 0.0, pytest.approx(3.142)]
+
+
+def test_errors_are_reported(tmp_path):
+    rc, msg = dump(["x"], 1, tmp_path)
+    assert rc == 1 and "No configuration file" in msg
+    rc, msg = dump(["x", "-f", "missing"], 1 | 2, tmp_path)
+    assert rc == 1 and "Failed to open config file" in msg
+    bad = tmp_path / "bad"
+    bad.write_text("files\np(1,1,1) r(1,0,0,0) a.pdb named\nsegments\nother 1 2 3\n")
+    rc, msg = dump(["x", "-f", "bad"], 1 | 2, tmp_path)
+    assert rc == 1 and "unknown molecule" in msg

@@ -1,0 +1,98 @@
+"""The C++ Simulation (argfile -> GPU engine -> reference output files) on a GB300.
+
+Input: the reference's own REMC regression configuration (tests/remctestfile: ubiquitin
+with a flexible tail and an all-flexible UIM in a 160.7 A box, 5 replicas 240-420 K,
+1000 MC steps, 100 exchange blocks, sampling every 10 steps) with the reference's
+parameter files and structures (fixtures).  The reference's seeded outputs
+(tests/remctest_{CPU,GPU}.tgz) give the file layout, which must match exactly, and one
+sample each of the acceptance and exchange statistics, which must fall within the
+spread of independent runs here (the random streams differ: GSL MT19937 there,
+Philox here).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import cgppd_gb300
+from helpers import write_reference_data_dir
+
+pytestmark = pytest.mark.gpu
+
+
+def run_sim(workdir, argv):
+    L = cgppd_gb300.lib()
+    f = L.cgppd_simulation_main
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]
+    arr = (ctypes.c_char_p * (len(argv) + 1))(*[a.encode() for a in argv], None)
+    old = os.getcwd()
+    os.chdir(workdir)
+    try:
+        return f(len(argv), arr, 0)
+    finally:
+        os.chdir(old)
+
+
+def parse_rows(path):
+    lines = open(path).read().splitlines()
+    rows = [ln for ln in lines if ":" in ln and not ln.startswith("Iteration")]
+    return lines, [[float(x) for x in ln.split(":", 1)[1].replace("|", " ").split()] for ln in rows]
+
+
+@pytest.fixture(scope="module")
+def workdir(tmp_path_factory, refdata):
+    d = tmp_path_factory.mktemp("remc")
+    write_reference_data_dir(str(d), refdata)
+    return d
+
+
+def config(refdata, prefix, seed):
+    text = refdata["remctestfile"].replace("prefix remctest", "prefix %s\nseed %d" % (prefix, seed))
+    return text
+
+
+def test_output_files_match_reference_layout(workdir, refdata):
+    (workdir / "remc_a").write_text(config(refdata, "remctest", 11))
+    assert run_sim(workdir, ["cgppd", "-f", "remc_a"]) == 0
+    out = workdir / "output" / "remctest_0"
+    gold = refdata["remctest"]["CPU"]
+    acc_lines, acc = parse_rows(out / "acceptance_ratios")
+    assert acc_lines[:2] == gold["acceptance_header"]
+    assert len(acc) == gold["acceptance_rows"] == 100
+    fb_lines, fb = parse_rows(out / "fractionBound")
+    assert fb_lines[:3] == gold["fraction_header"]
+    ex = open(out / "exchange_freq").read().splitlines()
+    assert ex[0] == "# Iteration continous_ratio, inst_ratio" and len(ex) - 1 == gold["exchange_rows"]
+    assert open(out / "fileindex").read().splitlines() == gold["fileindex"]
+    assert open(out / "boundconformations").read().splitlines()[:2] == gold["boundconformations_header"]
+    # row labels: MC step counts of the blocks, then the closing row
+    labels = [int(ln.split(":")[0]) for ln in acc_lines[2:] if ":" in ln]
+    assert labels == list(range(10, 1001, 10))
+    assert (out / "pdb" / "final_lowest_temperature.pdb").exists()
+
+
+def test_statistics_within_spread_of_reference(workdir, refdata):
+    finals, exch, fbound = [], [], []
+    for seed in range(1, 33):
+        prefix = "stat%d" % seed
+        (workdir / prefix).write_text(config(refdata, prefix, seed))
+        assert run_sim(workdir, ["cgppd", "-f", prefix]) == 0
+        out = workdir / "output" / (prefix + "_0")
+        _, acc = parse_rows(out / "acceptance_ratios")
+        finals.append(acc[-1][1::2])
+        _, fb = parse_rows(out / "fractionBound")
+        fbound.append(fb[-1][1::2])
+        exch.append(float(open(out / "exchange_freq").read().splitlines()[-1].split()[1]))
+    finals = np.array(finals)
+    mean, sd = finals.mean(0), finals.std(0, ddof=1)
+    em, es = np.mean(exch), np.std(exch, ddof=1)
+    for arch in ("CPU", "GPU"):
+        g = refdata["remctest"][arch]
+        ref_acc = np.array(g["acceptance_final_cumulative"])
+        z = np.abs(ref_acc - mean) / np.maximum(sd, 0.01)
+        assert np.all(z < 4.5), (arch, ref_acc, mean, sd)
+        assert abs(g["exchange_final_cumulative"] - em) / max(es, 0.01) < 4.5, (arch, g["exchange_final_cumulative"],
+                                                                                  em, es)
+        assert np.allclose(np.array(g["fraction_final_cumulative"]), np.mean(fbound, 0), atol=0.05)
