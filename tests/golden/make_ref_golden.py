@@ -4,8 +4,11 @@
 Runs the reference's energy code (oracle/_ref/libcgppd_ref.so, built from the
 reference tree by oracle/build_ref.py; available only where the tree is mounted) on
 the seeded initial structures of configurations c0, c1, c2 and c4, and on a few
-rigid-body perturbations of each, and writes tests/golden/ref_energies.json.  The GPU
-tests compare the engine against these numbers on a machine without the tree.
+rigid-body perturbations of each, and writes tests/golden/ref_energies.json.  The
+structures themselves go to tests/golden/ref_structures.npz: the seeded generator is
+not bit-reproducible across CPU architectures and numpy builds, so the tests read the
+exact inputs the energies were computed from.  The GPU tests compare the engine
+against these numbers on a machine without the tree.
 
 Usage: python tests/golden/make_ref_golden.py
 """
@@ -18,10 +21,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
 
 import oracle  # noqa: E402
 from oracle import ref  # noqa: E402
 from cgppd_gb300 import workloads  # noqa: E402
+from helpers import STRUCTURES, fixture_workload, save_structures  # noqa: E402
 
 
 def total_kcal(raw5, flexible):
@@ -49,8 +54,11 @@ def main():
     assert ref.available(), "the reference tree is needed to build oracle/_ref"
     out = {"source": "reference energy code (src/Potential.cpp, Residue.cpp, Geometry.cpp, ...) via "
                      "oracle/ref_harness.cpp", "configs": {}}
-    for cfg in ("c0", "c1", "c2", "c4"):
-        wl = workloads.make(cfg)
+    cfgs = ("c0", "c1", "c2", "c4")
+    save_structures(STRUCTURES, {cfg: workloads.make(cfg) for cfg in cfgs})
+    print("wrote", STRUCTURES, os.path.getsize(STRUCTURES), "bytes")
+    for cfg in cfgs:
+        wl = fixture_workload(cfg)
         sim = wl.sims[0]
         rng = np.random.default_rng(99)
         states = []

@@ -70,6 +70,56 @@ def write_reference_data_dir(root, refdata):
         write_pdb(os.path.join(d, "application", name + ".pdb"), refdata["pdbs"]["application/" + name]["residues"])
 
 
+STRUCTURES = os.path.join(ROOT, "tests", "golden", "ref_structures.npz")
+
+
+def save_structures(path, workloads_by_config):
+    """Write the first simulation of each seeded workload (molecules, box, contact and
+    torsion tables) to one .npz, so that fixtures computed from them do not depend on
+    regenerating the structures bit for bit on another machine."""
+    arrays = {}
+    for cfg, wl in workloads_by_config.items():
+        sim = wl.sims[0]
+        arrays[cfg + "/box"] = np.float64(sim.box)
+        arrays[cfg + "/lj_raw"] = wl.lj_raw
+        if wl.torsion_V is not None:
+            arrays[cfg + "/torsion_V"] = np.asarray(wl.torsion_V, np.float64)
+            arrays[cfg + "/torsion_phase"] = np.asarray(wl.torsion_phase, np.float64)
+        arrays[cfg + "/n_mol"] = np.int32(len(sim.molecules))
+        for k, m in enumerate(sim.molecules):
+            p = "%s/m%d/" % (cfg, k)
+            arrays[p + "xyz"] = m.xyz
+            arrays[p + "types"] = m.types.astype(np.uint8)
+            arrays[p + "charges"] = m.charges.astype(np.int8)
+            arrays[p + "radii"] = m.radii
+            arrays[p + "flags"] = np.array([m.all_flexible, m.crowder], np.uint8)
+            arrays[p + "segments"] = np.array([len(m.segments)] + [len(s) for s in m.segments] +
+                                              [v for s in m.segments for v in s], np.int32)
+    np.savez_compressed(path, **arrays)
+
+
+def fixture_workload(cfg, path=STRUCTURES):
+    """The workload of `cfg` as saved by save_structures (one simulation, one replica)."""
+    from cgppd_gb300 import workloads
+    z = np.load(path)
+    mols = []
+    for k in range(int(z[cfg + "/n_mol"])):
+        p = "%s/m%d/" % (cfg, k)
+        seg = z[p + "segments"].tolist()       # [count, lengths..., residues...]
+        segments, i = [], 1 + seg[0]
+        for n in seg[1:1 + seg[0]]:
+            segments.append(seg[i:i + n])
+            i += n
+        fl = z[p + "flags"]
+        mols.append(workloads.Molecule(z[p + "xyz"], z[p + "types"].astype(np.int32),
+                                       z[p + "charges"].astype(np.float32), z[p + "radii"], segments,
+                                       bool(fl[0]), bool(fl[1])))
+    V = z[cfg + "/torsion_V"] if cfg + "/torsion_V" in z else None
+    S = z[cfg + "/torsion_phase"] if cfg + "/torsion_phase" in z else None
+    sim = workloads.Simulation(mols, float(z[cfg + "/box"]), [300.0], [2.0], [0.2])
+    return workloads.Workload(cfg, [sim], z[cfg + "/lj_raw"], V, S)
+
+
 def header_functions():
     """Function names declared in include/*.h."""
     names = []

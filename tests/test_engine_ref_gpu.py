@@ -1,8 +1,9 @@
 """The engine's energies against the reference's own energy code.
 
 tests/golden/ref_energies.json holds totals the reference's energy code produced
-(tests/golden/make_ref_golden.py) for the synthetic configurations' initial states and
-rigid perturbations of them; the engine must reproduce each within 1e-5 relative.
+(tests/golden/make_ref_golden.py) for the synthetic configurations' initial states
+(saved in tests/golden/ref_structures.npz) and rigid perturbations of them; the engine
+must reproduce each within 1e-5 relative.
 """
 import json
 import os
@@ -12,6 +13,7 @@ import pytest
 
 from cgppd_gb300 import engine as eng
 from cgppd_gb300 import workloads
+from helpers import fixture_workload
 from test_ref_pin import perturbed
 
 pytestmark = pytest.mark.gpu
@@ -21,7 +23,7 @@ GOLD = json.load(open(os.path.join(HERE, "golden", "ref_energies.json")))
 
 @pytest.mark.parametrize("cfg", ["c0", "c1", "c2", "c4"])
 def test_engine_matches_reference_energies(cfg):
-    wl = workloads.make(cfg)
+    wl = fixture_workload(cfg)
     sim = wl.sims[0]
     for st in GOLD["configs"][cfg]:
         mols = perturbed(sim, st["transforms"])

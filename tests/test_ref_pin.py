@@ -2,7 +2,8 @@
 
 * Everywhere: the committed fixtures tests/golden/ref_energies.json (energies the
   reference's own energy code produced for the synthetic configurations, made by
-  tests/golden/make_ref_golden.py) against the oracle in reference precision (to
+  tests/golden/make_ref_golden.py, on the structures saved beside them in
+  tests/golden/ref_structures.npz) against the oracle in reference precision (to
   1e-9 relative) and in FP64 (1e-5).
 * Where the reference tree is mounted (oracle/_ref built from its sources): the same
   comparisons live, the reference's Graph::init against the oracle's and the
@@ -19,6 +20,7 @@ import oracle
 from cgppd_gb300 import workloads
 from oracle import ref
 from oracle.remc import OracleRemc
+from helpers import fixture_workload
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = json.load(open(os.path.join(HERE, "golden", "ref_energies.json")))
@@ -47,7 +49,7 @@ def oracle_energy(wl, sim, mols, mode):
 
 @pytest.mark.parametrize("cfg", ["c0", "c1", "c2", "c4"])
 def test_oracle_matches_reference_fixtures(cfg):
-    wl = workloads.make(cfg)
+    wl = fixture_workload(cfg)
     sim = wl.sims[0]
     for st in GOLD["configs"][cfg]:
         mols = perturbed(sim, st["transforms"])
