@@ -108,58 +108,103 @@ def contact_table(rng, ntypes=20, with_crowder=False, crowder_eps=0.1):
     return raw_from_epsilon(eps)
 
 
-def compact_chain(rng, n, radius=None, min_sep=4.0, tries=300):
-    """Self-avoiding walk of n residues, 3.8 A bonds, inside a sphere; centred on 0."""
+def _norm3(v):
+    """Euclidean length of a 3-vector in plain IEEE double arithmetic.  The generator
+    avoids BLAS (np.linalg.norm, @) so that a seed gives the same structures on every
+    CPU architecture and numpy build."""
+    x, y, z = float(v[0]), float(v[1]), float(v[2])
+    return math.sqrt(x * x + y * y + z * z)
+
+
+def _min_d2(P, k, p):
+    """Smallest squared distance from p to rows 0..k-1 of P (elementwise arithmetic)."""
+    if k <= 0:
+        return 1e18
+    dx = P[:k, 0] - p[0]
+    dy = P[:k, 1] - p[1]
+    dz = P[:k, 2] - p[2]
+    return float((dx * dx + dy * dy + dz * dz).min())
+
+
+def _centre(P):
+    c = [math.fsum(P[:, j].tolist()) / len(P) for j in range(3)]
+    return P - np.array(c)
+
+
+def _apply(X, R):
+    """Rows of X rotated by R (X @ R.T written out elementwise)."""
+    return X[:, 0:1] * R[:, 0] + X[:, 1:2] * R[:, 1] + X[:, 2:3] * R[:, 2]
+
+
+def _mat3(A, B):
+    return A[:, 0:1] * B[0:1, :] + A[:, 1:2] * B[1:2, :] + A[:, 2:3] * B[2:3, :]
+
+
+def _unit_step(rng, length, bias=None, spread=1.0):
+    d = rng.normal(size=3) * spread
+    if bias is not None:
+        d = d + bias
+    return d * (length / _norm3(d))
+
+
+def _first_free(P, k, cand, r_max, min_sep):
+    """Index of the first row of cand within r_max of the origin and at least min_sep
+    from rows 0..k-1 of P, or -1 (elementwise arithmetic throughout)."""
+    ok = cand[:, 0] * cand[:, 0] + cand[:, 1] * cand[:, 1] + cand[:, 2] * cand[:, 2] <= r_max * r_max
+    if k > 0:
+        dx = P[:k, 0][None, :] - cand[:, 0:1]
+        dy = P[:k, 1][None, :] - cand[:, 1:2]
+        dz = P[:k, 2][None, :] - cand[:, 2:3]
+        ok &= (dx * dx + dy * dy + dz * dz).min(1) >= min_sep * min_sep
+    idx = np.flatnonzero(ok)
+    return int(idx[0]) if len(idx) else -1
+
+
+def compact_chain(rng, n, radius=None, min_sep=4.0, tries=320, block=16):
+    """Self-avoiding walk of n residues, 3.8 A bonds, inside a sphere; centred on 0.
+    Each step draws candidate bond directions `block` at a time and keeps the first
+    one that stays in the sphere and clear of the chain."""
     if radius is None:
         radius = 12.0 * (n / 76.0) ** (1.0 / 3.0)
+    P = np.zeros((n, 3))
     for attempt in range(100):
         if attempt % 5 == 4:  # long chains jam in the sphere: loosen it a little
             radius *= 1.08
-        pts = [np.zeros(3)]
         ok = True
         for k in range(1, n):
-            placed = False
-            for _t in range(tries):
-                d = rng.normal(size=3)
-                d *= BOND / np.linalg.norm(d)
-                p = pts[-1] + d
-                if np.linalg.norm(p) > radius:
-                    continue
-                if k >= 2:
-                    prev = np.array(pts[:-1])
-                    if np.min(np.linalg.norm(prev - p, axis=1)) < min_sep:
-                        continue
-                pts.append(p)
-                placed = True
-                break
-            if not placed:
+            for _t in range(0, tries, block):
+                d = rng.normal(size=(block, 3))
+                nrm = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+                cand = P[k - 1] + d * (BOND / nrm)[:, None]
+                j = _first_free(P, k - 1, cand, radius, min_sep)
+                if j >= 0:
+                    P[k] = cand[j]
+                    break
+            else:
                 ok = False
                 break
         if ok:
-            xyz = np.array(pts)
-            return (xyz - xyz.mean(0)).astype(np.float32)
+            return _centre(P).astype(np.float32)
     raise RuntimeError("could not grow a compact chain of %d residues" % n)
-
-
-def _min_dist(pts, p):
-    return float(np.min(np.linalg.norm(np.asarray(pts) - p, axis=1))) if len(pts) else 1e9
 
 
 def two_domain_linker(rng, na, nl, nb, clearance=4.0):
     """Domain a, a self-avoiding linker of nl residues grown outward from a's last
     residue, then domain b attached at the linker's end and turned away from a."""
+    c2 = clearance * clearance
     for _ in range(200):
         a = compact_chain(rng, na).astype(np.float64)
-        out = a[-1] / (np.linalg.norm(a[-1]) + 1e-9)
-        pts = list(a)
+        out = a[-1] / (_norm3(a[-1]) + 1e-9)
+        P = np.zeros((na + nl, 3))
+        P[:na] = a
+        k = na
         ok = True
-        for k in range(nl):
+        for _l in range(nl):
             for _t in range(500):
-                d = out + 0.7 * rng.normal(size=3)
-                d *= BOND / np.linalg.norm(d)
-                p = pts[-1] + d
-                if _min_dist(pts[:-1], p) >= clearance:
-                    pts.append(p)
+                p = P[k - 1] + _unit_step(rng, BOND, bias=out, spread=0.7)
+                if _min_d2(P, k - 1, p) >= c2:
+                    P[k] = p
+                    k += 1
                     break
             else:
                 ok = False
@@ -167,30 +212,29 @@ def two_domain_linker(rng, na, nl, nb, clearance=4.0):
         if not ok:
             continue
         b = compact_chain(rng, nb).astype(np.float64)
-        head = np.array(pts[-1])
+        head = P[k - 1].copy()
         for _t in range(500):
             u = out + 0.5 * rng.normal(size=3)
-            u /= np.linalg.norm(u)
+            u = u / _norm3(u)
             R = rotation_between(-b[0], u)
             Q = rotation_between(np.array([1.0, 0, 0]), rng.normal(size=3))  # spin about the axis
-            bb = (b - b[0]) @ Q.T
-            bb = bb @ R.T
+            bb = _apply(_apply(b - b[0], Q), R)
             bb = bb - bb[0] + head + BOND * u
-            if min(_min_dist(pts[:-1], q) for q in bb) >= clearance and np.linalg.norm(bb[0] - head) > 3.7:
-                return np.concatenate([np.array(pts), bb]).astype(np.float32)
+            if min(_min_d2(P, k - 1, q) for q in bb) >= c2 and _norm3(bb[0] - head) > 3.7:
+                return np.concatenate([P, bb]).astype(np.float32)
     raise RuntimeError("could not build the two-domain linker structure")
 
 
 def rotation_between(v1, v2):
     """Rotation matrix taking direction v1 onto direction v2 (Rodrigues)."""
-    a = np.asarray(v1, np.float64) / np.linalg.norm(v1)
-    b = np.asarray(v2, np.float64) / np.linalg.norm(v2)
-    v = np.cross(a, b)
-    c = float(np.dot(a, b))
-    if np.linalg.norm(v) < 1e-12:
+    a = np.asarray(v1, np.float64) / _norm3(v1)
+    b = np.asarray(v2, np.float64) / _norm3(v2)
+    v = np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]])
+    c = float(a[0] * b[0] + a[1] * b[1] + a[2] * b[2])
+    if _norm3(v) < 1e-12:
         return np.eye(3) if c > 0 else -np.eye(3)
     K = np.array([[0, -v[2], v[1]], [v[2], 0, -v[0]], [-v[1], v[0], 0]])
-    return np.eye(3) + K + K @ K * (1.0 / (1.0 + c))
+    return np.eye(3) + K + _mat3(K, K) * (1.0 / (1.0 + c))
 
 
 def residue_params(rng, n, sigma_type, charged=True):
@@ -204,23 +248,25 @@ def residue_params(rng, n, sigma_type, charged=True):
 
 def place_centres(rng, radii, box, tries=10000):
     """Non-overlapping centres in the box (minimum image), largest first."""
-    order = np.argsort(-np.asarray(radii))
+    order = np.argsort(-np.asarray(radii), kind="stable")
     centres = [None] * len(radii)
-    placed = []
+    C = np.zeros((len(radii), 3))
+    rad = np.zeros(len(radii))
+    k = 0
     for i in order:
         for _ in range(tries):
             c = rng.uniform(0, box, 3)
-            good = True
-            for (pc, pr) in placed:
-                d = c - pc
-                d -= box * np.round(d / box)
-                if np.linalg.norm(d) < radii[i] + pr + 4.0:
-                    good = False
-                    break
-            if good:
-                centres[i] = c
-                placed.append((c, radii[i]))
-                break
+            if k:
+                d = C[:k] - c
+                d = d - box * np.round(d / box)
+                d2 = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2]
+                lim = rad[:k] + radii[i] + 4.0
+                if np.any(d2 < lim * lim):
+                    continue
+            centres[i] = c
+            C[k], rad[k] = c, radii[i]
+            k += 1
+            break
         else:
             raise RuntimeError("could not place molecule %d" % i)
     return centres
