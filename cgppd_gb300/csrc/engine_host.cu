@@ -16,12 +16,18 @@
 
 #include "cgppd_common.cuh"
 #include "cgppd_remc.h"
+#include "cgppd_surrogate.h"
+#include "devbuf.h"
 #include "engine_types.h"
 #include "host/graph.h"
 #include "status.h"
+#include "surrogate.cuh"
+#include "surrogate_internal.h"
 
 namespace cgppd {
-size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible);
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible, int da);
+cudaError_t launch_pose_samples(const EngineArgs &a, const int4 *items, int n, uint32_t key0, uint32_t key1, float *X,
+                                float *Y, cudaStream_t stream);
 cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
                             cudaStream_t stream);
 cudaError_t set_mc_smem_limit(size_t smem);
@@ -55,40 +61,53 @@ struct HostSim {
     std::vector<HostMolecule> mols;
 };
 
-template <typename T>
-struct DevBuf {
-    T *ptr = nullptr;
-    size_t n = 0;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (ptr)
-            cudaFree(ptr);
-        ptr = nullptr;
-        n = 0;
-    }
-    int alloc(size_t count)
-    {
-        release();
-        n = std::max<size_t>(count, 1);
-        return cgppd_check(cudaMalloc(&ptr, n * sizeof(T)), "engine allocation");
-    }
-    int upload(const std::vector<T> &v)
-    {
-        if (alloc(v.size()) != 0)
-            return -1;
-        if (v.empty())
-            return cgppd_check(cudaMemset(ptr, 0, sizeof(T)), "engine memset");
-        return cgppd_check(cudaMemcpy(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "engine upload");
-    }
-    int zero(size_t count)
-    {
-        if (alloc(count) != 0)
-            return -1;
-        return cgppd_check(cudaMemset(ptr, 0, n * sizeof(T)), "engine memset");
-    }
-};
 
+
+// Residues spanning a molecule's body frame, from its centred coordinates: the one
+// farthest from the centre, the one farthest from it, and the one farthest from the line
+// through both (lowest index on ties), so copies of one molecule pick the same residues.
+void frame_residues(const HostMolecule &hm, int &f0, int &f1, int &f2)
+{
+    f0 = f1 = f2 = 0;
+    if (hm.n < 3)
+        return;
+    auto q = [&](int i, int k) { return (double)hm.rel[3 * i + k]; };
+    double best = -1.0;
+    for (int i = 0; i < hm.n; ++i) {
+        const double d = q(i, 0) * q(i, 0) + q(i, 1) * q(i, 1) + q(i, 2) * q(i, 2);
+        if (d > best)
+            best = d, f0 = i;
+    }
+    best = -1.0;
+    for (int i = 0; i < hm.n; ++i) {
+        double d = 0.0;
+        for (int k = 0; k < 3; ++k)
+            d += (q(i, k) - q(f0, k)) * (q(i, k) - q(f0, k));
+        if (d > best)
+            best = d, f1 = i;
+    }
+    double u[3], nu = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        u[k] = q(f1, k) - q(f0, k);
+        nu += u[k] * u[k];
+    }
+    nu = std::sqrt(nu);
+    for (int k = 0; k < 3; ++k)
+        u[k] /= (nu > 0.0 ? nu : 1.0);
+    best = -1.0;
+    for (int i = 0; i < hm.n; ++i) {
+        double v[3], dot = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            v[k] = q(i, k) - q(f0, k);
+            dot += v[k] * u[k];
+        }
+        double d = 0.0;
+        for (int k = 0; k < 3; ++k)
+            d += (v[k] - dot * u[k]) * (v[k] - dot * u[k]);
+        if (d > best)
+            best = d, f2 = i;
+    }
+}
 
 }  // namespace
 
@@ -108,6 +127,14 @@ struct cgppd_engine {
     int max_n = 0, max_m = 0, max_mol = 0;
     int resident = 0, any_flexible = 0;
     int resident_pref = 1;
+    // delayed acceptance
+    cgppd_surrogate *sur = nullptr;
+    int da = 0;
+    float sur_thr = 0.5f, sur_window = 25.0f;
+    int sur_min = 100;
+    int plain_cluster = 1, plain_threads = 256;
+    DevBuf<int> d_sim_da;
+    DevBuf<DAStats> d_dastats;
     int report_capacity = 0;
     int last_launches = 0;
 
@@ -202,6 +229,14 @@ struct cgppd_engine {
         a.max_mol = max_mol;
         a.resident = resident;
         a.any_flexible = any_flexible;
+        a.da = da;
+        a.sur_P = surrogate_device_params(sur);
+        a.sur_wf = surrogate_device_wf(sur);
+        a.sim_da = d_sim_da.ptr;
+        a.dastats = d_dastats.ptr;
+        a.sur_thr2 = sur_thr * sur_thr;
+        a.sur_window = sur_window;
+        a.sur_min = sur_min;
         return a;
     }
 
@@ -310,6 +345,7 @@ int cgppd_engine::build()
             DevMol dm{};
             dm.start = start;
             dm.count = hm.n;
+            frame_residues(hm, dm.fr0, dm.fr1, dm.fr2);
             dm.flags = (flexible ? kMolFlexible : 0) | (hm.crowder ? kMolCrowder : 0);
             for (int i = 0; i < hm.n; ++i) {
                 float4 r4;
@@ -480,9 +516,11 @@ static void configure_shape(cgppd_engine *e, int C, int T)
 {
     e->cluster = C;
     e->threads = T;
-    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible);
-    e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024;
-    e->smem = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, e->resident, e->any_flexible);
+    const int da = e->da;
+    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, da);
+    const size_t s_da = da ? s_res - engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, 0) : 0;
+    e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024 + s_da;
+    e->smem = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, e->resident, e->any_flexible, da);
 }
 
 // Autotuner: time k_mc for each candidate launch shape on scratch copies of the mutable
@@ -492,7 +530,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
 {
     static std::map<std::vector<long long>, std::pair<int, int>> cache;
     std::vector<long long> key{e->total_replicas, e->max_n, e->max_m, e->max_mol, e->any_flexible, e->resident_pref,
-                               fixed_cluster, fixed_threads};
+                               fixed_cluster, fixed_threads, e->da};
     for (const auto &s : e->h_sims)
         key.push_back(((long long)s.N << 32) | ((long long)s.M << 16) | s.R);
     auto hit = cache.find(key);
@@ -515,19 +553,26 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
         clone(in, e->d_intra) || clone(pot, e->d_potential) || clone(st, e->d_stats) || clone(sc, e->d_stepc) ||
         clone(pc, e->d_pairc) || clone(ef, e->d_errflags))
         return -1;
+    DevBuf<DAStats> das;
+    if (e->da && clone(das, e->d_dastats))
+        return -1;
     EngineArgs base = e->args();
     base.pos = pos.ptr, base.rel = rel.ptr, base.center = cen.ptr, base.emat = em.ptr, base.intra = in.ptr;
     base.potential = pot.ptr, base.stats = st.ptr, base.stepc = sc.ptr, base.pairc = pc.ptr, base.errflags = ef.ptr;
+    if (e->da)
+        base.dastats = das.ptr;
     const int clusters[4] = {1, 2, 4, 8}, thread_opts[2] = {128, 256};
     const int steps = 32;
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
     float best = 1e30f;
-    int bc = 1, bt = 256;
+    int bc = e->da ? 8 : 1, bt = 256;
     e->tuning.clear();
     for (int C : clusters) {
         if (fixed_cluster > 0 && C != fixed_cluster)
+            continue;
+        if (e->da && C < 4)  // the surrogate's weights are split over 4 or 8 CTAs
             continue;
         for (int T : thread_opts) {
             if (fixed_threads > 0 && T != fixed_threads)
@@ -675,7 +720,7 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
         return -1;
     const bool tune = cluster <= 0 || threads <= 0;
     configure_shape(e, std::min(8, std::max(1, cluster > 0 ? cluster : 1)), threads == 128 ? 128 : 256);
-    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0);
     if (std::max(e->smem, s_init) > 227 * 1024)
         return cgppd_fail("cgppd_engine_finalize: system too large for shared memory (reduce molecule size or N)");
     if (cgppd_check(set_mc_smem_limit(std::max(e->smem, s_init)), "engine shared-memory limit") != 0)
@@ -690,6 +735,10 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
         return -1;
     if (tune && autotune(e, cluster, threads) != 0)
         return -1;
+    if (e->d_sim_da.zero(e->sims.size()) != 0 || e->d_dastats.zero((size_t)e->total_replicas) != 0)
+        return -1;
+    e->plain_cluster = e->cluster;
+    e->plain_threads = e->threads;
     e->finalized = true;
     return 0;
 }
@@ -824,7 +873,7 @@ int cgppd_engine_recompute(cgppd_engine *e, double *out, int write_state)
     if (cgppd_check(cudaStreamSynchronize(e->own_stream), "recompute") != 0)
         return -1;
     EngineArgs a = e->args();
-    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0);
     double *dst = write_state ? e->d_potential.ptr : e->d_scratch_pot.ptr;
     if (!write_state) {
         // evaluate into scratch copies so the running state is untouched
@@ -954,7 +1003,7 @@ int cgppd_engine_upload(cgppd_engine *e, int sim, const float *pos4, const float
         rc |= cgppd_check(cudaMemcpyAsync(e->d_center.ptr + S.molst_off, centers4, sizeof(float4) * S.M * S.R,
                                           cudaMemcpyHostToDevice, st), "upload centres");
     if (rc == 0 && recompute) {
-        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible);
+        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0);
         rc |= cgppd_check(launch_init_energy(e->args(), e->total_replicas, s_init, e->d_potential.ptr, st),
                           "upload recompute");
     }
@@ -1064,6 +1113,156 @@ int cgppd_engine_launch_shape(const cgppd_engine *e, int *cluster, int *threads)
     if (threads)
         *threads = e->threads;
     return e->resident;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ learned surrogate
+
+// Every molecule a rigid, non-crowder copy of the first (count, types, charges, radii and
+// frame residues), 2..64 molecules of at least 3 residues.
+static bool sim_compatible(const cgppd_engine *e, int sim)
+{
+    const HostSim &hs = e->sims[sim];
+    const int M = (int)hs.mols.size();
+    if (M < 2 || M > 64)
+        return false;
+    const HostMolecule &m0 = hs.mols[0];
+    const int mol_off = e->h_sims[sim].mol_off;
+    const DevMol &d0 = e->h_mols[mol_off];
+    if (m0.n < 3)
+        return false;
+    for (int k = 0; k < M; ++k) {
+        const HostMolecule &mk = hs.mols[k];
+        const DevMol &dk = e->h_mols[mol_off + k];
+        if (mk.crowder || (dk.flags & kMolFlexible))
+            return false;
+        if (mk.n != m0.n || mk.types != m0.types || mk.charges != m0.charges || mk.radii != m0.radii)
+            return false;
+        if (dk.fr0 != d0.fr0 || dk.fr1 != d0.fr1 || dk.fr2 != d0.fr2)
+            return false;
+    }
+    return true;
+}
+
+extern "C" {
+
+int cgppd_engine_surrogate_compatible(cgppd_engine *e, int sim)
+{
+    if (!e || !e->finalized || sim < 0 || sim >= (int)e->sims.size())
+        return cgppd_fail("cgppd_engine_surrogate_compatible: bad engine or simulation index");
+    return sim_compatible(e, sim) ? 1 : 0;
+}
+
+int cgppd_engine_set_surrogate(cgppd_engine *e, cgppd_surrogate *s, float rmse_threshold, float error_window,
+                               int min_evals)
+{
+    if (!e || !e->finalized)
+        return cgppd_fail("cgppd_engine_set_surrogate: engine not finalized");
+    if (s && (!(rmse_threshold > 0.f) || !(error_window > 0.f) || min_evals < 1))
+        return cgppd_fail("cgppd_engine_set_surrogate: threshold and window must be positive, min_evals >= 1");
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "set surrogate") != 0)
+        return -1;
+    std::vector<int> on(e->sims.size(), 0);
+    int count = 0;
+    if (s)
+        for (size_t k = 0; k < e->sims.size(); ++k) {
+            on[k] = sim_compatible(e, (int)k) ? 1 : 0;
+            count += on[k];
+        }
+    if (e->d_sim_da.upload(on) != 0 || e->d_dastats.zero((size_t)e->total_replicas) != 0)
+        return -1;
+    e->da = count > 0 ? 1 : 0;
+    e->sur = e->da ? s : nullptr;
+    if (s) {
+        e->sur_thr = rmse_threshold;
+        e->sur_window = error_window;
+        e->sur_min = min_evals;
+    }
+    for (auto &kv : e->graphs)
+        cudaGraphExecDestroy(kv.second);
+    e->graphs.clear();
+    if (e->da) {
+        if (autotune(e, 0, 0) != 0)
+            return -1;
+    } else {
+        configure_shape(e, e->plain_cluster, e->plain_threads);
+    }
+    if (e->smem > 227 * 1024)
+        return cgppd_fail("cgppd_engine_set_surrogate: the screened kernel does not fit in shared memory");
+    if (cgppd_check(set_mc_smem_limit(e->smem), "engine shared-memory limit") != 0)
+        return -1;
+    return count;
+}
+
+int cgppd_engine_surrogate_stats(cgppd_engine *e, int sim, double *out)
+{
+    if (!e || !e->finalized || sim < 0 || sim >= (int)e->sims.size() || !out)
+        return cgppd_fail("cgppd_engine_surrogate_stats: bad argument");
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "surrogate stats") != 0)
+        return -1;
+    const DevSim &S = e->h_sims[sim];
+    for (int k = 0; k < 7; ++k)
+        out[k] = 0.0;
+    if (!e->da)
+        return 0;
+    std::vector<DAStats> d(S.R);
+    int flag = 0;
+    if (cgppd_check(cudaMemcpy(d.data(), e->d_dastats.ptr + S.rep_off, sizeof(DAStats) * S.R, cudaMemcpyDeviceToHost),
+                    "surrogate stats") != 0 ||
+        cgppd_check(cudaMemcpy(&flag, e->d_sim_da.ptr + sim, sizeof(int), cudaMemcpyDeviceToHost), "surrogate flag"))
+        return -1;
+    for (const DAStats &x : d) {
+        out[0] += (double)x.proposals;
+        out[1] += (double)x.stage1_reject;
+        out[2] += (double)x.stage2_eval;
+        out[3] += (double)x.stage2_accept;
+        out[4] += x.sum_e2;
+        out[5] += (double)x.n_e2;
+    }
+    out[6] = flag;
+    return 0;
+}
+
+int cgppd_surrogate_collect(cgppd_surrogate *s, cgppd_engine *e, int sim, int n, double proposal_fraction,
+                            unsigned long long seed)
+{
+    if (!s || !e || !e->finalized || sim < 0 || sim >= (int)e->sims.size() || n <= 0)
+        return cgppd_fail("cgppd_surrogate_collect: bad argument");
+    if (!sim_compatible(e, sim))
+        return cgppd_fail("cgppd_surrogate_collect: the simulation is not made of copies of one rigid molecule");
+    const DevSim &S = e->h_sims[sim];
+    uint64_t rs = seed;
+    auto next = [&rs]() {
+        uint64_t z = (rs += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    std::vector<int4> items(n);
+    for (int i = 0; i < n; ++i) {
+        const int g = S.rep_off + (int)(next() % (uint64_t)S.R);
+        int a = (int)(next() % (uint64_t)S.M), b = (int)(next() % (uint64_t)(S.M - 1));
+        if (b >= a)
+            ++b;
+        if (a > b)
+            std::swap(a, b);
+        const double u = (double)(next() >> 11) * (1.0 / 9007199254740992.0);
+        const int mode = (u < proposal_fraction) ? 1 + (int)(next() & 1) : 0;
+        items[i] = make_int4(g, a, b, mode);
+    }
+    DevBuf<int4> d_items;
+    DevBuf<float> dX, dY;
+    if (d_items.upload(items) != 0 || dX.alloc((size_t)n * kSurIn) != 0 || dY.alloc((size_t)n) != 0)
+        return -1;
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "collect") != 0)
+        return -1;
+    const uint32_t k0 = (uint32_t)(seed ^ 0x51A7u), k1 = (uint32_t)(seed >> 32) ^ 0x2545F491u;
+    if (cgppd_check(launch_pose_samples(e->args(), d_items.ptr, n, k0, k1, dX.ptr, dY.ptr, e->own_stream),
+                    "pose samples") != 0 ||
+        cgppd_check(cudaStreamSynchronize(e->own_stream), "pose samples") != 0)
+        return -1;
+    return surrogate_append_device_samples(s, dX.ptr, dY.ptr, n);
 }
 
 }  // extern "C"

@@ -32,6 +32,7 @@
 
 #include "cgppd_common.cuh"
 #include "engine_types.h"
+#include "surrogate.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -52,18 +53,28 @@ struct MoveDesc {
     float wcx, wcy, wcz;     // centre after the move (wrapped)
     float px, py, pz;        // flex pivot position
     uint32_t w_metro;
+    uint32_t w_stage1;       // delayed acceptance: the surrogate stage's uniform draw
 };
 
 struct SmemLayout {
     int table, mols, ipos, irel, iexcl, idisp, iq, ej, rowp, row;    // always
     int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM;                        // resident only
+    int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
     int total;
 };
+
+// Delayed acceptance: each CTA of a replica's cluster holds the output columns
+// [rank * S, rank * S + S) of layers 1..4 (S = 256 / C); rows of the pose batch are
+// padded to multiples of 16 (one mma.sync m-tile); BF16 rows are padded to 264 elements
+// so that the fragment loads of 8 consecutive rows hit distinct banks.
+constexpr int kDaWS = kSurH + 8;
+
+__host__ __device__ inline int da_rows(int max_m) { return (((max_m - 1 > 1 ? max_m - 1 : 1) + 15) / 16) * 16; }
 
 __host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
 
 __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int max_m, int max_n, int resident,
-                                                  int any_flexible)
+                                                  int any_flexible, int da = 0, int C = 1)
 {
     SmemLayout L;
     int off = 0;
@@ -88,14 +99,28 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
         L.INTRA = off;  off = align16(off + 8 * max_m);
         L.ROWSUM = off; off = align16(off + 8 * max_m);
     }
+    L.daW = L.daW1 = L.daB = L.daW5 = L.daH = L.daHS = L.daX = L.daP = L.daF = L.daSM = 0;
+    if (da) {
+        const int S = kSurH / C, RP = da_rows(max_m);
+        L.daW = off;   off += 3 * S * kDaWS * 2;
+        L.daW1 = off;  off += S * kSurIn * 4;
+        L.daB = off;   off += 4 * S * 4;
+        L.daW5 = off;  off = align16(off + S * 4);
+        L.daH = off;   off += RP * kDaWS * 2;
+        L.daHS = off;  off += 2 * RP * S * 2;
+        L.daX = off;   off += RP * kSurIn * 4;
+        L.daP = off;   off += RP * 4;
+        L.daF = off;   off = align16(off + RP * 4);
+        L.daSM = off;  off = align16(off + 4 * max_m * max_m);
+    }
     L.total = off;
     return L;
 }
 
-size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible)
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible, int da)
 {
     const int slice = (max_n + cluster - 1) / cluster;
-    return (size_t)smem_layout(max_mol, slice, max_m, max_n, resident, any_flexible).total;
+    return (size_t)smem_layout(max_mol, slice, max_m, max_n, resident, any_flexible, da, cluster).total;
 }
 
 // ------------------------------------------------------------------ helpers
@@ -405,11 +430,239 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, const DevMol *
     }
     }
     mv.w_metro = w[8];
+    mv.w_stage1 = w[9];
+}
+
+// ------------------------------------------------------------------ surrogate screening
+//
+// Delayed acceptance (two-stage Metropolis): stage 1 accepts a proposal with
+// min(1, exp(-beta dS)), dS = the surrogate's change of sum_{a<b} f(pose_ab); only
+// stage-1 survivors are evaluated exactly, and stage 2 accepts them with
+// min(1, exp(-beta (dE - dS))).  The product of the two is a Metropolis-Hastings kernel
+// for the exact Boltzmann distribution.  f of every pair is kept in SM (shared memory,
+// rebuilt at each launch with the same code that scores proposals), so dS needs only
+// the moved molecule's M - 1 new poses: one batch of the MLP per proposal, split over
+// the replica's cluster by output columns with activations exchanged through DSMEM.
+
+struct DaView {
+    __nv_bfloat16 *W;   // [3][S][kDaWS] rows = this CTA's output units of layers 2..4
+    float *W1;          // [S][8]
+    float *B;           // [4][S] biases of layers 1..4
+    float *W5;          // [S]
+    __nv_bfloat16 *H;   // [RP][kDaWS] full activations of the previous layer
+    __nv_bfloat16 *hs;  // [2][RP][S] this CTA's outputs (double buffer)
+    float *X;           // [RP][8] pose features
+    float *P;           // [RP] partial outputs of this CTA
+    float *F;           // [RP] predictions
+    float *SM;          // [M][M] f of every pair
+    float b5;
+    int S, RP;
+};
+
+__device__ DaView da_view(unsigned char *smem, const SmemLayout &Ly, int C, int max_m)
+{
+    DaView v;
+    v.W = reinterpret_cast<__nv_bfloat16 *>(smem + Ly.daW);
+    v.W1 = reinterpret_cast<float *>(smem + Ly.daW1);
+    v.B = reinterpret_cast<float *>(smem + Ly.daB);
+    v.W5 = reinterpret_cast<float *>(smem + Ly.daW5);
+    v.H = reinterpret_cast<__nv_bfloat16 *>(smem + Ly.daH);
+    v.hs = reinterpret_cast<__nv_bfloat16 *>(smem + Ly.daHS);
+    v.X = reinterpret_cast<float *>(smem + Ly.daX);
+    v.P = reinterpret_cast<float *>(smem + Ly.daP);
+    v.F = reinterpret_cast<float *>(smem + Ly.daF);
+    v.SM = reinterpret_cast<float *>(smem + Ly.daSM);
+    v.S = kSurH / C;
+    v.RP = da_rows(max_m);
+    v.b5 = 0.f;
+    return v;
+}
+
+// This CTA's slices of the parameters (once per launch).
+__device__ void da_load_weights(const EngineArgs &a, DaView &v, int rank, int t, int T)
+{
+    const int S = v.S, c0 = rank * S;
+    const uint4 *wf = reinterpret_cast<const uint4 *>(a.sur_wf);
+    for (int idx = t; idx < 3 * S * 32; idx += T) {
+        const int l = idx / (S * 32), rem = idx - l * S * 32, r = rem >> 5, q = rem & 31;
+        *reinterpret_cast<uint4 *>(v.W + ((size_t)l * S + r) * kDaWS + q * 8) = wf[((size_t)l * kSurH + c0 + r) * 32 + q];
+    }
+    for (int idx = t; idx < S * kSurIn; idx += T)
+        v.W1[idx] = a.sur_P[kOffW1 + c0 * kSurIn + idx];
+    for (int idx = t; idx < 4 * S; idx += T) {
+        const int l = idx / S, c = idx - l * S;
+        v.B[idx] = a.sur_P[sur_b_off(l + 1) + c0 + c];
+    }
+    for (int c = t; c < S; c += T)
+        v.W5[c] = a.sur_P[kOffW5 + c0 + c];
+    v.b5 = a.sur_P[kOffB5];
+}
+
+// Predictions F[0..R) of the pose rows X[0..R) (R <= RP).  Every CTA of the cluster
+// ends with the same values.  Holds cluster barriers: call uniformly across the cluster.
+__device__ void da_eval(DaView &v, int R, int C, int t, int T)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    const int S = v.S, RPc = ((R + 15) >> 4) << 4;
+    const int warp = t >> 5, lane = t & 31, NW = T >> 5;
+    __nv_bfloat16 *cur = v.hs, *nxt = v.hs + v.RP * S;
+    // layer 1 in FP32 (same operation order as the training kernel)
+    for (int idx = t; idx < RPc * S; idx += T) {
+        const int j = idx / S, c = idx - j * S;
+        float z = v.B[c];
+#pragma unroll
+        for (int i = 0; i < kSurIn; ++i)
+            z = fmaf(v.W1[c * kSurIn + i], v.X[j * kSurIn + i], z);
+        cur[idx] = __float2bfloat16_rn(silu(z));
+    }
+    cl.sync();
+    for (int layer = 2; layer <= 4; ++layer) {
+        // all 256 inputs of this layer, gathered from the cluster in rank order
+        for (int idx = t; idx < RPc * 32; idx += T) {
+            const int j = idx >> 5, col = (idx & 31) * 8, r = col / S, c = col - r * S;
+            const __nv_bfloat16 *src = cl.map_shared_rank(cur, r) + j * S + c;
+            *reinterpret_cast<uint4 *>(v.H + j * kDaWS + col) = *reinterpret_cast<const uint4 *>(src);
+        }
+        __syncthreads();
+        const __nv_bfloat16 *Wl = v.W + (size_t)(layer - 2) * S * kDaWS;
+        const float *bl = v.B + (layer - 1) * S;
+        const int mt = RPc >> 4, nt = S >> 3, g = lane >> 2, tig = lane & 3;
+        for (int task = warp; task < mt * nt; task += NW) {
+            const int tm = task / nt, tn = task - tm * nt;
+            const int r0 = tm * 16 + g, n = tn * 8 + g;
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+            for (int kt = 0; kt < kSurH / 16; ++kt) {
+                const int k0 = kt * 16 + 2 * tig;
+                uint32_t af[4], bf[2];
+                af[0] = *reinterpret_cast<const uint32_t *>(v.H + r0 * kDaWS + k0);
+                af[1] = *reinterpret_cast<const uint32_t *>(v.H + (r0 + 8) * kDaWS + k0);
+                af[2] = *reinterpret_cast<const uint32_t *>(v.H + r0 * kDaWS + k0 + 8);
+                af[3] = *reinterpret_cast<const uint32_t *>(v.H + (r0 + 8) * kDaWS + k0 + 8);
+                bf[0] = *reinterpret_cast<const uint32_t *>(Wl + n * kDaWS + k0);
+                bf[1] = *reinterpret_cast<const uint32_t *>(Wl + n * kDaWS + k0 + 8);
+                mma_bf16_16816(d, af, bf);
+            }
+            const int col = tn * 8 + 2 * tig;
+            *reinterpret_cast<uint32_t *>(nxt + r0 * S + col) =
+                pack_bf16(silu(d[0] + bl[col]), silu(d[1] + bl[col + 1]));
+            *reinterpret_cast<uint32_t *>(nxt + (r0 + 8) * S + col) =
+                pack_bf16(silu(d[2] + bl[col]), silu(d[3] + bl[col + 1]));
+        }
+        __nv_bfloat16 *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        if (layer < 4)
+            cl.sync();
+    }
+    __syncthreads();
+    for (int j = t; j < RPc; j += T) {
+        float s = 0.f;
+        for (int c = 0; c < S; ++c)
+            s = fmaf(__bfloat162float(cur[j * S + c]), v.W5[c], s);
+        v.P[j] = s;
+    }
+    cl.sync();
+    for (int j = t; j < R; j += T) {
+        float f = 0.f;
+        for (int r = 0; r < C; ++r)
+            f += cl.map_shared_rank(v.P, r)[j];
+        v.F[j] = f + v.b5;
+    }
+    __syncthreads();
+}
+
+template <bool RES>
+__device__ __forceinline__ Frame mol_frame(const float4 *Q, const DevMol &mb)
+{
+    return frame_from(ld_state<RES>(&Q[mb.start + mb.fr0]), ld_state<RES>(&Q[mb.start + mb.fr1]),
+                      ld_state<RES>(&Q[mb.start + mb.fr2]));
+}
+
+__device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
+
+// Pose rows of the proposal: the moved molecule (new centre and frame) against every
+// other molecule, ordered pairs (lower index first); rows up to the next multiple of 16
+// are zeroed.
+template <bool RES>
+__device__ void da_step_features(const DevMol *mols, const float4 *Q, const float4 *CEN, const MoveDesc &mv, int M,
+                                 float box, float invbox, float *X, int t, int T)
+{
+    const int R = M - 1, RPc = ((R + 15) >> 4) << 4;
+    for (int j = t; j < RPc; j += T) {
+        float *x = X + j * kSurIn;
+        if (j >= R) {
+#pragma unroll
+            for (int i = 0; i < kSurIn; ++i)
+                x[i] = 0.f;
+            continue;
+        }
+        const int b = (j < mv.m) ? j : j + 1;
+        const DevMol &mm = mols[mv.m];
+        float4 q[3] = {ld_state<RES>(&Q[mm.start + mm.fr0]), ld_state<RES>(&Q[mm.start + mm.fr1]),
+                       ld_state<RES>(&Q[mm.start + mm.fr2])};
+        if (mv.type == kRotate)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float3 rr = rot_apply(mv.R, q[k].x, q[k].y, q[k].z);
+                q[k] = make_float4(rr.x, rr.y, rr.z, 0.f);
+            }
+        const Frame Fm = frame_from(q[0], q[1], q[2]);
+        const Frame Fb = mol_frame<RES>(Q, mols[b]);
+        const float3 cm = make_float3(mv.wcx, mv.wcy, mv.wcz), cb = f3(ld_state<RES>(&CEN[b]));
+        if (mv.m < b)
+            pair_features(Fm, cm, Fb, cb, box, invbox, x);
+        else
+            pair_features(Fb, cb, Fm, cm, box, invbox, x);
+    }
+}
+
+// SM[a][b] = f(pose_ab) for every pair of the current state, in chunks of RP rows.
+template <bool RES>
+__device__ void da_init_matrix(DaView &v, const DevMol *mols, const float4 *Q, const float4 *CEN, int M, float box,
+                               float invbox, int C, int t, int T)
+{
+    const int npairs = M * (M - 1) / 2;
+    for (int p0 = 0; p0 < npairs; p0 += v.RP) {
+        const int R = min(v.RP, npairs - p0);
+        for (int j = t; j < v.RP; j += T) {
+            float *x = v.X + j * kSurIn;
+            if (j >= R) {
+                for (int i = 0; i < kSurIn; ++i)
+                    x[i] = 0.f;
+                continue;
+            }
+            int pa = 0, rem = p0 + j;
+            while (rem >= M - 1 - pa) {
+                rem -= M - 1 - pa;
+                ++pa;
+            }
+            const int pb = pa + 1 + rem;
+            pair_features(mol_frame<RES>(Q, mols[pa]), f3(ld_state<RES>(&CEN[pa])), mol_frame<RES>(Q, mols[pb]),
+                          f3(ld_state<RES>(&CEN[pb])), box, invbox, x);
+        }
+        __syncthreads();
+        da_eval(v, R, C, t, T);
+        for (int j = t; j < R; j += T) {
+            int pa = 0, rem = p0 + j;
+            while (rem >= M - 1 - pa) {
+                rem -= M - 1 - pa;
+                ++pa;
+            }
+            const int pb = pa + 1 + rem;
+            v.SM[pa * M + pb] = v.F[j];
+            v.SM[pb * M + pa] = v.F[j];
+        }
+        __syncthreads();
+    }
+    for (int k = t; k < M; k += T)
+        v.SM[k * M + k] = 0.f;
+    __syncthreads();
 }
 
 // ------------------------------------------------------------------ MC kernel
 
-template <bool RES>
+template <bool RES, bool DA>
 __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -420,6 +673,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     __shared__ int s_accept;
     __shared__ DevSim S;           // this replica's simulation (read by thread 0 mostly)
     __shared__ ReplicaStats st;    // counters, updated by thread 0
+    __shared__ double s_ds;        // delayed acceptance: surrogate energy change of the proposal
+    __shared__ int s_skip;         // ... 1 when stage 1 rejected it
+    __shared__ DAStats s_da;
 
     const int C = a.cluster;
     const int t = threadIdx.x, T = blockDim.x, lane = t & 31, warp = t >> 5, NW = T >> 5;
@@ -431,12 +687,16 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     if (t == 0) {
         S = a.sims[s];
         st = a.stats[g];
+        if (DA)
+            s_da = a.dastats[g];
     }
     __syncthreads();
     const int r = g - S.rep_off;
     const int N = S.N, M = S.M;
     const int slice = (a.max_n + C - 1) / C;
-    const SmemLayout Ly = smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible);
+    const SmemLayout Ly = smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible, DA ? 1 : 0, C);
+    // screening is on for this simulation (uniform over the cluster: one simulation)
+    const bool da_on = DA && a.sim_da[s] != 0;
     float *s_table = reinterpret_cast<float *>(smem + Ly.table);
     DevMol *s_mols = reinterpret_cast<DevMol *>(smem + Ly.mols);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
@@ -512,6 +772,16 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     if (t == 0)
         s_pot = __ldcg(&a.potential[g]);
     __syncthreads();
+    DaView dv;
+    if (DA) {
+        dv = da_view(smem, Ly, C, a.max_m);
+        if (da_on) {
+            da_load_weights(a, dv, rank, t, T);
+            __syncthreads();
+            da_init_matrix<RES>(dv, s_mols, Q, CEN, M, L, invL, C, t, T);
+            cg::this_cluster().sync();  // no CTA leaves while another reads its shared memory
+        }
+    }
 
     for (int step = 0; step < nsteps; ++step) {
         const unsigned long long mcstep = step0 + (unsigned long long)step;
@@ -539,6 +809,40 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const bool nullm = mv.null_move != 0;
         const bool flexmol = mv.flexible != 0;
 
+        // ---- delayed acceptance, stage 1: the surrogate's energy change of the proposal
+        const bool screened = da_on && !nullm && !flexmol;
+        bool skip = false;
+        if (DA && screened) {
+            da_step_features<RES>(s_mols, Q, CEN, mv, M, L, invL, dv.X, t, T);
+            __syncthreads();
+            da_eval(dv, M - 1, C, t, T);
+            if (t == 0) {
+                double fnew = 0.0, fold = 0.0;
+                for (int j = 0; j < M - 1; ++j) {
+                    const int b = (j < m) ? j : j + 1;
+                    fnew += (double)dv.F[j];
+                    fold += (double)dv.SM[m * M + b];
+                }
+                const double ds = fnew - fold;
+                s_ds = ds;
+                const float dsf = (float)ds;
+                int pass = 1;
+                if (!(dsf < 0.0f)) {
+                    const float boltz = expf(-(dsf * kKcal) / (kRgas * temperature));
+                    pass = ((double)mv.w_stage1 < (double)boltz * 4294967296.0) ? 1 : 0;
+                }
+                s_skip = !pass;
+                s_da.proposals++;
+                if (!pass) {
+                    s_da.stage1_reject++;
+                    st.reject++;
+                }
+            }
+            __syncthreads();
+            skip = s_skip != 0;
+        }
+
+        if (!skip) {
         if (!RES && warp == 0) {
             // old row from the global matrix (read before anyone commits this step)
             double v = 0.0;
@@ -771,7 +1075,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 const double new_row = v + s_intra_new;
                 s_new_row = new_row;
                 const double newPotential = s_pot - s_old_row + new_row;
-                const float delta = (float)(newPotential - s_pot);
+                float delta = (float)(newPotential - s_pot);
+                if (DA && screened)  // stage 2: exact change less the surrogate's
+                    delta = (float)((newPotential - s_pot) - s_ds);
                 int acc = 0;
                 if (delta < 0.0f) {
                     acc = 1;
@@ -781,6 +1087,18 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 }
                 if (!isfinite(newPotential))
                     acc = 0;
+                if (DA && screened) {
+                    const double dE = newPotential - s_pot, e = dE - s_ds;
+                    s_da.stage2_eval++;
+                    if (acc)
+                        s_da.stage2_accept++;
+                    if (fabs(dE) <= (double)a.sur_window && isfinite(e)) {
+                        s_da.sum_e2 += e * e;
+                        s_da.n_e2++;
+                        s_da.win_e2 += e * e;
+                        s_da.win_n++;
+                    }
+                }
                 s_accept = acc;
                 if (acc)
                     s_pot = newPotential;
@@ -825,6 +1143,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             if (t == 0)
                 CEN[m] = make_float4(mv.wcx, mv.wcy, mv.wcz, 0.f);
         }
+        if (DA && screened && acc) {  // every CTA keeps its own copy of the surrogate matrix
+            for (int j = t; j < M - 1; j += T) {
+                const int b = (j < m) ? j : j + 1;
+                dv.SM[m * M + b] = dv.F[j];
+                dv.SM[b * M + m] = dv.F[j];
+            }
+        }
+        }  // !skip
         // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
         const int freq = S.sample_freq;
         if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&
@@ -873,6 +1199,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         if (t == 0) {
             a.potential[g] = s_pot;
             a.stats[g] = st;
+            if (DA)
+                a.dastats[g] = s_da;
             a.stepc[g] = step0 + (unsigned long long)nsteps;
             a.pairc[g] += pairs;
             if (errbits)
@@ -1023,6 +1351,21 @@ __global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block
     int *st = a.sim_state + 4 * s;
     const int x = st[1];
     const int R = S.R;
+    // delayed acceptance: fall back to the plain test when the surrogate's error over
+    // the block's second-stage evaluations drifts past the threshold
+    if (a.da && a.sim_da[s]) {
+        double e2 = 0.0;
+        unsigned long long cnt = 0;
+        for (int k = 0; k < R; ++k) {
+            DAStats &d = a.dastats[S.rep_off + k];
+            e2 += d.win_e2;
+            cnt += d.win_n;
+            d.win_e2 = 0.0;
+            d.win_n = 0;
+        }
+        if (cnt >= (unsigned long long)a.sur_min && e2 > (double)a.sur_thr2 * (double)cnt)
+            a.sim_da[s] = 0;
+    }
     // reporting happens when sampling has started (src/Simulation.cpp:751-768)
     if ((long long)steps_per_block * x >= (long long)S.sample_after && x < a.report_capacity) {
         for (int tt = 0; tt < R; ++tt) {
@@ -1086,7 +1429,109 @@ __global__ void k_final_report(EngineArgs a, int total_replicas, int row)
     }
 }
 
+// ------------------------------------------------------------------ surrogate samples
+
+// Training sample `si` = (replica g, molecules a < b, mode): the pose features of the
+// pair (a', b) and its exact inter-molecule energy, where a' is molecule a unchanged
+// (mode 0) or displaced by one MC proposal of replica g drawn from Philox (mode 1
+// translate by the replica's step along a cube-biased direction, mode 2 rotate by its
+// angle about such an axis; src/Molecule.cpp:193-221).
+__global__ void __launch_bounds__(128) k_pose_samples(EngineArgs a, const int4 *items, uint32_t key0, uint32_t key1,
+                                                      float *X, float *Y)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ FF s_red[kMaxWarps];
+    __shared__ float s_R[9], s_c[3];
+    const int si = blockIdx.x, t = threadIdx.x, T = blockDim.x;
+    const int4 it = items[si];
+    const int g = it.x, ma = it.y, mb = it.z, mode = it.w;
+    const DevSim S = a.sims[a.rep_sim[g]];
+    const int r = g - S.rep_off, N = S.N, M = S.M;
+    const DevMol A = a.mols[S.mol_off + ma], B = a.mols[S.mol_off + mb];
+    const long long st0 = S.state_off + (long long)r * N;
+    const float4 *Q = a.rel + st0, *P = a.pos + st0;
+    const float4 *CEN = a.center + S.molst_off + (long long)r * M;
+    const float4 *stat = a.rstat + S.res_off;
+    float *s_table = reinterpret_cast<float *>(smem);
+    float4 *s_pa = reinterpret_cast<float4 *>(smem + kTableStride * kTableStride * 4);
+    float2 *s_qa = reinterpret_cast<float2 *>(smem + kTableStride * kTableStride * 4 + 16 * a.max_mol);
+    const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
+    for (int k = t; k < kTableStride * kTableStride; k += T)
+        s_table[k] = a.table[k];
+    if (t == 0) {
+        const float4 c = CEN[ma];
+        float R[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+        float cx = c.x, cy = c.y, cz = c.z;
+        if (mode != 0) {
+            const U4 w = philox4x32_10(U4{(uint32_t)si, 0u, 0u, 0x504Fu}, key0, key1);
+            const float3 u = normalized(centred(w.x, false), centred(w.y, true), centred(w.z, false));
+            if (mode == 1) {
+                const float ts = a.tstep[g];
+                cx = wrapf(c.x + u.x * ts, L);
+                cy = wrapf(c.y + u.y * ts, L);
+                cz = wrapf(c.z + u.z * ts, L);
+            } else {
+                axis_angle_matrix((float)a.rstep[g], u.x, u.y, u.z, true, R);
+            }
+        }
+        for (int k = 0; k < 9; ++k)
+            s_R[k] = R[k];
+        s_c[0] = cx, s_c[1] = cy, s_c[2] = cz;
+    }
+    __syncthreads();
+    for (int i = t; i < A.count; i += T) {
+        const float4 q = Q[A.start + i];
+        const float3 rr = (mode == 2) ? rot_apply(s_R, q.x, q.y, q.z) : make_float3(q.x, q.y, q.z);
+        const float4 sr = stat[A.start + i];
+        s_pa[i] = make_float4(s_c[0] + rr.x, s_c[1] + rr.y, s_c[2] + rr.z, sr.x);
+        s_qa[i] = make_float2(sr.y, sr.z);
+    }
+    __syncthreads();
+    FF acc{0.f, 0.f};
+    for (int jj = t; jj < B.count; jj += T) {
+        const int j = B.start + jj;
+        const float4 pj = P[j], sj = stat[j];
+        const float4 rj = make_float4(pj.x, pj.y, pj.z, sj.x);
+        const float2 qj = make_float2(sj.y, sj.z);
+        float part = 0.f;
+        for (int i = 0; i < A.count; ++i) {
+            part += pair_kcal(s_pa[i], s_qa[i], rj, qj, s_table, L, invL);
+            if ((i & 31) == 31) {
+                ff_add(acc, part);
+                part = 0.f;
+            }
+        }
+        ff_add(acc, part);
+    }
+    const double e = block_sum_ff(acc, s_red);
+    if (t == 0) {
+        Y[si] = (float)e;
+        float4 q[3] = {Q[A.start + A.fr0], Q[A.start + A.fr1], Q[A.start + A.fr2]};
+        if (mode == 2)
+            for (int k = 0; k < 3; ++k) {
+                const float3 rr = rot_apply(s_R, q[k].x, q[k].y, q[k].z);
+                q[k] = make_float4(rr.x, rr.y, rr.z, 0.f);
+            }
+        const Frame Fa = frame_from(q[0], q[1], q[2]);
+        const Frame Fb = frame_from(Q[B.start + B.fr0], Q[B.start + B.fr1], Q[B.start + B.fr2]);
+        pair_features(Fa, make_float3(s_c[0], s_c[1], s_c[2]), Fb, f3(CEN[mb]), L, invL, X + (size_t)si * kSurIn);
+    }
+}
+
 // ------------------------------------------------------------------ launchers
+
+cudaError_t launch_pose_samples(const EngineArgs &a, const int4 *items, int n, uint32_t key0, uint32_t key1, float *X,
+                                float *Y, cudaStream_t stream)
+{
+    const size_t smem = (size_t)kTableStride * kTableStride * 4 + 24 * (size_t)a.max_mol;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_pose_samples, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    k_pose_samples<<<n, 128, smem, stream>>>(a, items, key0, key1, X, Y);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
                             cudaStream_t stream)
@@ -1104,9 +1549,14 @@ cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = (C > 1) ? 1 : 0;
+    if (a.da) {
+        if (a.resident)
+            return cudaLaunchKernelEx(&cfg, k_mc<true, true>, a, nsteps);
+        return cudaLaunchKernelEx(&cfg, k_mc<false, true>, a, nsteps);
+    }
     if (a.resident)
-        return cudaLaunchKernelEx(&cfg, k_mc<true>, a, nsteps);
-    return cudaLaunchKernelEx(&cfg, k_mc<false>, a, nsteps);
+        return cudaLaunchKernelEx(&cfg, k_mc<true, false>, a, nsteps);
+    return cudaLaunchKernelEx(&cfg, k_mc<false, false>, a, nsteps);
 }
 
 cudaError_t set_mc_smem_limit(size_t smem)
@@ -1117,9 +1567,13 @@ cudaError_t set_mc_smem_limit(size_t smem)
     if (smem <= s_max)
         return cudaSuccess;
     s_max = smem;
-    cudaError_t e = cudaFuncSetAttribute(k_mc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_mc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_mc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_init_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return e;

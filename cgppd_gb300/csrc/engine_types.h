@@ -58,6 +58,16 @@ struct DevMol {
     int local_off, nlocal;
     int crank_off, ncrank;
     int nintra;                  // intra pairs that are not excluded (flexible molecules)
+    int fr0, fr1, fr2;           // residues (molecule-relative) spanning the body frame
+};
+
+// Delayed-acceptance counters of one replica slot (not swapped on exchange).
+struct DAStats {
+    unsigned long long proposals, stage1_reject, stage2_eval, stage2_accept;
+    double sum_e2;               // squared (exact - surrogate) energy changes, |exact| <= window
+    unsigned long long n_e2;
+    double win_e2;               // the same since the last fallback check
+    unsigned long long win_n;
 };
 
 // Per-replica counters and ratios, swapped with the temperature on exchange
@@ -118,6 +128,15 @@ struct EngineArgs {
     int max_n;                   // largest N
     int max_m;                   // largest M
     int max_mol;                 // largest molecule
+    // delayed acceptance with the learned surrogate (da != 0: k_mc<.., true> is launched)
+    int da;
+    const float *sur_P;          // FP32 master parameters
+    const void *sur_wf;          // BF16 Wf[3][256][256] of layers 2..4
+    int *sim_da;                 // per simulation: 1 while screening, 0 after a fallback
+    DAStats *dastats;            // per replica slot
+    float sur_thr2;              // fallback when mean squared error > sur_thr2
+    float sur_window;            // errors counted for |exact change| <= sur_window
+    int sur_min;                 // ... once a block has at least sur_min of them
 };
 
 }  // namespace cgppd

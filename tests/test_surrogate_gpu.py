@@ -1,0 +1,182 @@
+"""The learned pair-energy surrogate on a GB300: kernels against the CPU oracle, training,
+and delayed-acceptance screening inside the engine.
+
+* forward pass and loss gradient of the tcgen05 training kernels against the float64
+  restatement (oracle/mlp.py), both with the GPU's bfloat16 rounding points emulated
+  (tight) and as the exact float64 network (loose);
+* training samples: pose features and exact pair energies produced by the engine against
+  the oracle's features and FP64 pair energies of the same states;
+* screening with a network that predicts exactly zero leaves the trajectory identical
+  to the plain engine (stage 1 always passes, stage 2 is the plain test);
+* an untrained network trips the error threshold and the simulation falls back;
+* training lowers the held-out error.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import mlp
+from cgppd_gb300 import engine as eng
+from cgppd_gb300 import surrogate as sg
+from cgppd_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def pose_like(rng, n):
+    X = np.zeros((n, 8), np.float32)
+    X[:, :3] = rng.normal(scale=1.2, size=(n, 3))
+    X[:, 3] = rng.uniform(0.15, 1.2, n)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1
+    X[:, 4:] = q
+    return X
+
+
+@pytest.fixture(scope="module")
+def net():
+    s = sg.Surrogate(batch=512, seed=7)
+    yield s
+    s.close()
+
+
+def test_forward_matches_oracle(net):
+    rng = np.random.default_rng(1)
+    X = pose_like(rng, 300)            # not a multiple of 128: padded inside
+    out = net.predict(X)
+    p = net.params.astype(np.float64)
+    ref_bf, _ = mlp.forward(p, X, bf16_path=True)
+    ref64, _ = mlp.forward(p, X)
+    assert np.max(np.abs(out - ref_bf)) <= 2e-3 * (1 + np.max(np.abs(ref_bf))), np.max(np.abs(out - ref_bf))
+    assert rel_err(out, ref64) < 3e-2
+
+
+def test_gradients_match_oracle(net):
+    rng = np.random.default_rng(2)
+    X = pose_like(rng, 512)
+    y = rng.normal(size=512).astype(np.float32)
+    loss, g = net.loss_grad(X, y)
+    p = net.params.astype(np.float64)
+    lb, gb = mlp.loss_grad(p, X, y, bf16_path=True)
+    l64, g64 = mlp.loss_grad(p, X, y)
+    assert loss == pytest.approx(lb, rel=2e-3)
+    assert loss == pytest.approx(l64, rel=2e-2)
+    for k, (o, n) in mlp.OFF.items():
+        assert rel_err(g[o:o + n], gb[o:o + n]) < 2e-2, (k, rel_err(g[o:o + n], gb[o:o + n]))
+        assert rel_err(g[o:o + n], g64[o:o + n]) < 8e-2, (k, rel_err(g[o:o + n], g64[o:o + n]))
+    cos = float(np.dot(g, g64) / (np.linalg.norm(g) * np.linalg.norm(g64)))
+    assert cos > 0.998
+
+
+def subset(wl, nrep):
+    sim = wl.sims[0]
+    return workloads.Simulation(sim.molecules, sim.box, sim.temperatures[:nrep], sim.translate_steps[:nrep],
+                                sim.rotate_steps[:nrep], sim.move_weights, sim.rigid_rotate_prob)
+
+
+def engine_for(wl, sims, cluster=8, threads=256):
+    w2 = workloads.Workload(wl.name, sims, wl.lj_raw, wl.torsion_V, wl.torsion_phase, wl.seed)
+    return eng.from_workload(w2, cluster=cluster, threads=threads)
+
+
+def oracle_pair_energies(wl, sim, xyz):
+    mols = sim.molecules
+    start = np.cumsum([0] + [m.n for m in mols[:-1]]).astype(np.int32)
+    cnt = np.array([m.n for m in mols], np.int32)
+    aa = np.concatenate([m.types for m in mols])
+    q = np.concatenate([m.charges for m in mols])
+    s = np.concatenate([m.radii for m in mols])
+    return oracle.E_inter_matrix(oracle.FP64, xyz.astype(np.float32), aa, q, s, start, cnt, wl.lj_raw, sim.box)
+
+
+def test_training_samples_match_oracle():
+    wl = workloads.make("c4")
+    sim = subset(wl, 2)
+    e = engine_for(wl, [sim])
+    assert sg.compatible(e, 0)
+    e.run(2, 50)                      # two different replica states
+    s = sg.Surrogate(batch=128, seed=3)
+    s.collect(e, 0, 96, proposal_fraction=0.0, seed=11)
+    X, y = s.samples()
+    fr = mlp.frame_residues(sim.molecules[0].xyz - sim.molecules[0].xyz.mean(0))
+    cands = []
+    for r in range(2):
+        xyz, rel, cen = e.state(0, r)
+        E = oracle_pair_energies(wl, sim, xyz)
+        off = np.cumsum([0] + [m.n for m in sim.molecules])
+        frames = [mlp.frame(*rel[off[k] + np.array(fr)]) for k in range(len(sim.molecules))]
+        for a in range(len(sim.molecules)):
+            for b in range(a + 1, len(sim.molecules)):
+                cands.append((mlp.features(frames[a], cen[a], frames[b], cen[b], sim.box), E[a, b]))
+    CX = np.array([c[0] for c in cands])
+    CE = np.array([c[1] for c in cands])
+    for x, yy in zip(X, y):
+        d = np.max(np.abs(CX - x), axis=1)
+        k = int(np.argmin(d))
+        assert d[k] < 2e-4, d[k]
+        assert abs(yy - CE[k]) <= 1e-5 * abs(CE[k]) + 1e-6, (yy, CE[k])
+    s.close()
+    e.close()
+
+
+def run_pair(wl, nrep, blocks, steps, attach_with=None, **kw):
+    e = engine_for(wl, [subset(wl, nrep)])
+    if attach_with is not None:
+        assert sg.attach(e, attach_with, **kw) == 1
+    e.run(blocks, steps, exchange_after_last=True)
+    e.synchronize()
+    return e
+
+
+def test_zero_surrogate_reproduces_plain_trajectory():
+    wl = workloads.make("c4")
+    s = sg.Surrogate(batch=128, seed=5)
+    s.params = np.zeros(sg.N_PARAMS, np.float32)
+    plain = run_pair(wl, 4, 3, 100)
+    da = run_pair(wl, 4, 3, 100, attach_with=s, rmse_threshold=1e9)
+    rp, rd = plain.replicas(0), da.replicas(0)
+    for k in ("accept", "acceptA", "reject", "totalAccept", "totalAcceptReject", "label", "tindex"):
+        assert np.array_equal(rp[k], rd[k]), k
+    assert np.allclose(rp["potential"], rd["potential"], rtol=1e-9, atol=1e-9)
+    for r in range(4):
+        assert np.allclose(plain.state(0, r)[0], da.state(0, r)[0], atol=1e-4)
+    st = sg.stats(da, 0)
+    assert st["proposals"] == 4 * 300 and st["stage1_reject"] == 0 and st["stage2_eval"] == 4 * 300
+    assert st["screening"] == 1
+    plain.close()
+    da.close()
+    s.close()
+
+
+def test_untrained_surrogate_falls_back():
+    wl = workloads.make("c4")
+    s = sg.Surrogate(batch=128, seed=9)
+    p = s.params
+    p[mlp.OFF["b5"][0]] = 0.0
+    p[mlp.OFF["w5"][0]:mlp.OFF["w5"][0] + 256] *= 50.0     # wildly wrong pair energies
+    s.params = p
+    e = run_pair(wl, 4, 1, 200, attach_with=s, rmse_threshold=0.5, min_evals=10)
+    st = sg.stats(e, 0)
+    assert st["screening"] == 0 and st["rmse"] > 0.5
+    before = st["proposals"]
+    e.run(1, 100)
+    e.synchronize()
+    assert sg.stats(e, 0)["proposals"] == before     # plain steps from now on
+    e.close()
+    s.close()
+
+
+def test_training_lowers_heldout_error():
+    wl = workloads.make("c4")
+    e = engine_for(wl, [subset(wl, 8)])
+    s, hist = sg.train_on_engine(e, 0, n_samples=40960, blocks=4, steps_per_block=100, epochs=6, batch=1024)
+    assert s.n_samples == 40960
+    assert np.all(np.isfinite(hist))
+    assert hist[-1, 1] < hist[0, 1]
+    e.close()
+    s.close()
