@@ -48,6 +48,11 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--surrogate-workload", default="c4")
+    p.add_argument("--surrogate-samples", type=int, default=2_000_000)
+    p.add_argument("--surrogate-epochs", type=int, default=8)
+    p.add_argument("--surrogate-blocks", type=int, default=10, help="timed blocks of each surrogate-leg arm")
     return p.parse_args()
 
 
@@ -158,6 +163,70 @@ def reference_arm(args):
                                                                                  [r[1] for r in rates])},
            "e2e": {"value": value, "unit": "replica MC steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+# ------------------------------------------------------------------ surrogate leg
+
+def surrogate_leg(args, torch, flush):
+    """Plain vs surrogate-screened throughput on the identical-copies configuration: time
+    the plain engine, train the surrogate on (pose, exact energy) samples drawn from that
+    plain run, attach it, time the screened engine.  Both arms run the same workload from
+    the same starting state with the same Philox stream; the screened arm's statistics
+    are those of the exact distribution (delayed acceptance)."""
+    from cgppd_gb300 import engine as eng
+    from cgppd_gb300 import surrogate as sg
+    from cgppd_gb300 import workloads
+    wl = workloads.make(args.surrogate_workload)
+    K = args.block
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def timed(e, blocks):
+        with torch.cuda.stream(stream):
+            for _ in range(max(3, args.warmup)):
+                flush.fill_(1.0)
+                e.run(1, K, True, stream=sh)
+        torch.cuda.synchronize()
+        s0, p0 = e.counters()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            for _ in range(blocks):
+                flush.fill_(1.0)
+                e.run(1, K, True, stream=sh)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        s1, p1 = e.counters()
+        return (s1 - s0) / (ms / 1000.0), (p1 - p0) / max(1, s1 - s0), ms
+
+    plain = eng.from_workload(wl)
+    plain_rate, plain_pairs, _ = timed(plain, args.surrogate_blocks)
+    t0 = time.perf_counter()
+    s, hist = sg.train_on_engine(plain, 0, n_samples=args.surrogate_samples, blocks=20, steps_per_block=K,
+                                 epochs=args.surrogate_epochs, batch=8192, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    plain.close()
+    screened = eng.from_workload(wl)
+    n_on = sg.attach(screened, s, rmse_threshold=0.5)
+    st0 = sg.stats(screened, 0)
+    da_rate, da_pairs, _ = timed(screened, args.surrogate_blocks)
+    st = sg.stats(screened, 0)
+    d = {k: st[k] - st0.get(k, 0.0) for k in ("proposals", "stage1_reject", "stage2_eval", "stage2_accept")}
+    shape = screened.launch_shape()
+    out = {"workload": wl.name, "plain_replica_mc_steps_per_s": plain_rate,
+           "screened_replica_mc_steps_per_s": da_rate, "speedup": da_rate / plain_rate,
+           "exact_pairs_per_step_plain": plain_pairs, "exact_pairs_per_step_screened": da_pairs,
+           "stage1_reject_fraction": d["stage1_reject"] / max(1.0, d["proposals"]),
+           "stage2_accept_fraction": d["stage2_accept"] / max(1.0, d["stage2_eval"]),
+           "screened_proposals": d["proposals"], "online_rmse_kcal": st["rmse"], "still_screening": bool(st["screening"]),
+           "simulations_screened": n_on, "train_samples": s.n_samples, "train_epochs": args.surrogate_epochs,
+           "train_seconds_incl_sampling": train_s, "heldout_rmse_per_epoch": [float(x) for x in hist[:, 1]],
+           "cluster_ctas_per_replica": shape[0], "threads_per_cta": shape[1]}
+    screened.close()
+    s.close()
+    return out
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -277,6 +346,10 @@ def gpu_arm(args):
         cpu = {"value": rate, "unit": "replica MC steps/s", "cores": threads, "kind": "port",
                "sample": "%d replicas x %d MC steps of the same workload (%.1f s)" % (Rr, steps, dt)}
 
+    sur = None
+    if rank == 0 and world == 1 and not args.no_surrogate:
+        sur = surrogate_leg(args, torch, flush)
+
     props = torch.cuda.get_device_properties(local)
     clocks = clk.summary()
     max_mhz = clocks["sm_max_mhz"] or 2070.0
@@ -309,6 +382,7 @@ def gpu_arm(args):
                          "peak_note": "nominal FP32 pipe: SMs x 128 lanes x 2 x max SM clock (no FP32 figure in "
                                       "the measured peaks)"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "surrogate": sur,
         }
         print(json.dumps(out))
     if dist:

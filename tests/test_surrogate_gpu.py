@@ -153,20 +153,38 @@ def test_zero_surrogate_reproduces_plain_trajectory():
     s.close()
 
 
-def test_untrained_surrogate_falls_back():
+def test_error_threshold_falls_back_to_plain():
+    # a network predicting zero passes every proposal to stage 2, whose error is then the
+    # exact change itself: with a tiny threshold the simulation must fall back
     wl = workloads.make("c4")
     s = sg.Surrogate(batch=128, seed=9)
-    p = s.params
-    p[mlp.OFF["b5"][0]] = 0.0
-    p[mlp.OFF["w5"][0]:mlp.OFF["w5"][0] + 256] *= 50.0     # wildly wrong pair energies
-    s.params = p
-    e = run_pair(wl, 4, 1, 200, attach_with=s, rmse_threshold=0.5, min_evals=10)
+    s.params = np.zeros(sg.N_PARAMS, np.float32)
+    e = run_pair(wl, 4, 1, 200, attach_with=s, rmse_threshold=1e-6, min_evals=10)
     st = sg.stats(e, 0)
-    assert st["screening"] == 0 and st["rmse"] > 0.5
+    assert st["n_e2"] >= 10 and st["rmse"] > 1e-6
+    assert st["screening"] == 0
     before = st["proposals"]
     e.run(1, 100)
     e.synchronize()
     assert sg.stats(e, 0)["proposals"] == before     # plain steps from now on
+    e.close()
+    s.close()
+
+
+def test_bad_surrogate_keeps_exact_bookkeeping():
+    # a wildly wrong network only changes which proposals are tried exactly: the running
+    # totals still equal a fresh evaluation of the final coordinates
+    wl = workloads.make("c4")
+    s = sg.Surrogate(batch=128, seed=9)
+    p = s.params
+    p[mlp.OFF["w5"][0]:mlp.OFF["w5"][0] + 256] *= 50.0
+    s.params = p
+    e = run_pair(wl, 4, 2, 200, attach_with=s, rmse_threshold=1e9)
+    pot = e.replicas(0)["potential"]
+    assert np.allclose(e.recompute(False), pot, rtol=1e-6, atol=1e-6)
+    st = sg.stats(e, 0)
+    assert st["proposals"] == 4 * 400 and st["screening"] == 1
+    assert st["stage1_reject"] + st["stage2_eval"] == st["proposals"]
     e.close()
     s.close()
 
