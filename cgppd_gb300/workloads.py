@@ -188,10 +188,21 @@ def compact_chain(rng, n, radius=None, min_sep=4.0, tries=320, block=16):
     raise RuntimeError("could not grow a compact chain of %d residues" % n)
 
 
-def two_domain_linker(rng, na, nl, nb, clearance=4.0):
+def two_domain_linker(rng, na, nl, nb, clearance=6.0, min_sep=4.0):
     """Domain a, a self-avoiding linker of nl residues grown outward from a's last
-    residue, then domain b attached at the linker's end and turned away from a."""
-    c2 = clearance * clearance
+    residue, then domain b attached at the linker's end and turned away from a.
+    Residues four or more apart along the chain (the pairs that interact) keep
+    `clearance` between them; residues two or three apart keep `min_sep`."""
+    c2, s2 = clearance * clearance, min_sep * min_sep
+
+    def clear(P, k_end, i, p):
+        # candidate p at chain index i against rows 0..k_end-1 (chain indices 0..k_end-1)
+        far = min(i - 3, k_end)
+        if _min_d2(P, far, p) < c2:
+            return False
+        lo, hi = max(i - 3, 0), min(i - 1, k_end)
+        return hi <= lo or _min_d2(P[lo:], hi - lo, p) >= s2
+
     for _ in range(200):
         a = compact_chain(rng, na).astype(np.float64)
         out = a[-1] / (_norm3(a[-1]) + 1e-9)
@@ -202,7 +213,7 @@ def two_domain_linker(rng, na, nl, nb, clearance=4.0):
         for _l in range(nl):
             for _t in range(500):
                 p = P[k - 1] + _unit_step(rng, BOND, bias=out, spread=0.7)
-                if _min_d2(P, k - 1, p) >= c2:
+                if clear(P, k, k, p):
                     P[k] = p
                     k += 1
                     break
@@ -220,7 +231,7 @@ def two_domain_linker(rng, na, nl, nb, clearance=4.0):
             Q = rotation_between(np.array([1.0, 0, 0]), rng.normal(size=3))  # spin about the axis
             bb = _apply(_apply(b - b[0], Q), R)
             bb = bb - bb[0] + head + BOND * u
-            if min(_min_d2(P, k - 1, q) for q in bb) >= c2 and _norm3(bb[0] - head) > 3.7:
+            if all(clear(P, k, k + t, q) for t, q in enumerate(bb)) and _norm3(bb[0] - head) > 3.7:
                 return np.concatenate([P, bb]).astype(np.float32)
     raise RuntimeError("could not build the two-domain linker structure")
 

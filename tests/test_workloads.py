@@ -13,7 +13,7 @@ from cgppd_gb300 import workloads
 
 DIGESTS = {
     "c0": "273ff57466bcf611160d4f711cdf1da4dee4e7655d33c489fcfa5fa4de7b2074",
-    "c1": "ace95a9b785f00c7cf9c50165466be85c32974d5a1be2f90fa9c2a980f8eb864",
+    "c1": "66cab24931498384b1449a442aeb01d28fce95cbad3ad60fb26c3ae1e4ca5a56",
     "c2": "8ab60f3b4daaf4f98299baa4b4c2dd2173a4162f0f9c27cf1449ed3bea848a23",
     "c4": "c3b1b9132300771eb1e0f3cbae9a8121d6a3785e3471e1f1c2f4f72ba2fd3202",
 }
