@@ -25,7 +25,8 @@
 #include "surrogate_internal.h"
 
 namespace cgppd {
-size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible, int da);
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible, int da,
+                         const int *lmax);
 cudaError_t launch_pose_samples(const EngineArgs &a, const int4 *items, int n, uint32_t key0, uint32_t key1, float *X,
                                 float *Y, cudaStream_t stream);
 cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
@@ -125,6 +126,7 @@ struct cgppd_engine {
     size_t smem = 0;
     int total_replicas = 0;
     int max_n = 0, max_m = 0, max_mol = 0;
+    int lmax[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // largest per-simulation static list sizes
     int resident = 0, any_flexible = 0;
     int resident_pref = 1;
     // delayed acceptance
@@ -227,6 +229,8 @@ struct cgppd_engine {
         a.max_n = max_n;
         a.max_m = max_m;
         a.max_mol = max_mol;
+        for (int k = 0; k < 9; ++k)
+            a.lmax[k] = lmax[k];
         a.resident = resident;
         a.any_flexible = any_flexible;
         a.da = da;
@@ -301,6 +305,12 @@ int cgppd_engine::build()
         ds.sample_after = hs.p.sample_after;
         ds.bound_threshold = hs.p.bound_threshold;
 
+        auto list_sizes = [&]() {
+            return std::vector<int>{(int)bonds.size(), (int)angles.size(), (int)tors.size(), (int)indsub.size(),
+                                    (int)flexres.size(), (int)flexopt.size(), (int)branch.size(),
+                                    (int)localres.size(), (int)crankres.size()};
+        };
+        const std::vector<int> lbase = list_sizes();
         // replica-wide UIDs (Graph::assign_uids with running offsets, src/Replica.cpp:33-40)
         int chain_off = 1, dom_off = 1, bond_off = 1;
         int non_crowders = 0;
@@ -426,6 +436,12 @@ int cgppd_engine::build()
             start += hm.n;
             max_mol = std::max(max_mol, hm.n);
         }
+        const std::vector<int> lend = list_sizes();
+        for (int k = 0; k < 9; ++k) {
+            ds.lbase[k] = lbase[k];
+            ds.lcount[k] = lend[k] - lbase[k];
+            lmax[k] = std::max(lmax[k], ds.lcount[k]);
+        }
         ds.non_crowders = non_crowders;
         // Replica::sample chooses what the bound test compares (src/Replica.cpp:1043-1075)
         if (M == 1)
@@ -517,10 +533,10 @@ static void configure_shape(cgppd_engine *e, int C, int T)
     e->cluster = C;
     e->threads = T;
     const int da = e->da;
-    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, da);
-    const size_t s_da = da ? s_res - engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, 0) : 0;
+    const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, da, e->lmax);
+    const size_t s_da = da ? s_res - engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, 0, e->lmax) : 0;
     e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024 + s_da;
-    e->smem = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, e->resident, e->any_flexible, da);
+    e->smem = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, e->resident, e->any_flexible, da, e->lmax);
 }
 
 // Autotuner: time k_mc for each candidate launch shape on scratch copies of the mutable
@@ -720,7 +736,7 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
         return -1;
     const bool tune = cluster <= 0 || threads <= 0;
     configure_shape(e, std::min(8, std::max(1, cluster > 0 ? cluster : 1)), threads == 128 ? 128 : 256);
-    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0, nullptr);
     if (std::max(e->smem, s_init) > 227 * 1024)
         return cgppd_fail("cgppd_engine_finalize: system too large for shared memory (reduce molecule size or N)");
     if (cgppd_check(set_mc_smem_limit(std::max(e->smem, s_init)), "engine shared-memory limit") != 0)
@@ -873,7 +889,7 @@ int cgppd_engine_recompute(cgppd_engine *e, double *out, int write_state)
     if (cgppd_check(cudaStreamSynchronize(e->own_stream), "recompute") != 0)
         return -1;
     EngineArgs a = e->args();
-    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0);
+    const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0, nullptr);
     double *dst = write_state ? e->d_potential.ptr : e->d_scratch_pot.ptr;
     if (!write_state) {
         // evaluate into scratch copies so the running state is untouched
@@ -1003,7 +1019,7 @@ int cgppd_engine_upload(cgppd_engine *e, int sim, const float *pos4, const float
         rc |= cgppd_check(cudaMemcpyAsync(e->d_center.ptr + S.molst_off, centers4, sizeof(float4) * S.M * S.R,
                                           cudaMemcpyHostToDevice, st), "upload centres");
     if (rc == 0 && recompute) {
-        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0);
+        const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0, nullptr);
         rc |= cgppd_check(launch_init_energy(e->args(), e->total_replicas, s_init, e->d_potential.ptr, st),
                           "upload recompute");
     }

@@ -58,6 +58,8 @@ struct MoveDesc {
 
 struct SmemLayout {
     int table, mols, ipos, irel, iexcl, idisp, iq, ej, rowp, row;    // always
+    int rcv;                                                         // clusters: pushed partial rows
+    int lst[11];                                                     // resident + flexible: static lists
     int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM;                        // resident only
     int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
     int total;
@@ -73,8 +75,11 @@ __host__ __device__ inline int da_rows(int max_m) { return (((max_m - 1 > 1 ? ma
 
 __host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
 
+enum ListId { kLBond = 0, kLAng, kLTor, kLInd, kLFlex, kLFopt, kLBranch, kLLocal, kLCrank };
+
 __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int max_m, int max_n, int resident,
-                                                  int any_flexible, int da = 0, int C = 1)
+                                                  int any_flexible, int da = 0, int C = 1,
+                                                  const int *lmax = nullptr)
 {
     SmemLayout L;
     int off = 0;
@@ -88,6 +93,8 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     L.ej = off;     off = align16(off + 8 * slice);
     L.rowp = off;   off = align16(off + 8 * (max_m + 1));
     L.row = off;    off = align16(off + 8 * (max_m + 1));
+    // [2 step parities][C source ranks][max_m + 1] (last entry: internal energy)
+    L.rcv = off;    off = align16(off + (C > 1 ? 2 * C * (max_m + 1) * 8 : 0));
     L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = 0;
     if (resident) {
         L.P = off;      off += 16 * max_n;
@@ -98,6 +105,19 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
         L.EM = off;     off = align16(off + 8 * max_m * max_m);
         L.INTRA = off;  off = align16(off + 8 * max_m);
         L.ROWSUM = off; off = align16(off + 8 * max_m);
+    }
+    for (int k = 0; k < 11; ++k)
+        L.lst[k] = 0;
+    if (resident && any_flexible && lmax) {
+        // bonds, angles, torsions, torsion V, torsion phases, indirect pairs, flex residues,
+        // flex options, branch residues, local residues, crankshaft residues
+        const int bytes[11] = {8 * lmax[kLBond], 16 * lmax[kLAng], 16 * lmax[kLTor], 16 * lmax[kLTor],
+                               16 * lmax[kLTor], 8 * lmax[kLInd], 16 * lmax[kLFlex], 16 * lmax[kLFopt],
+                               4 * lmax[kLBranch], 4 * lmax[kLLocal], 4 * lmax[kLCrank]};
+        for (int k = 0; k < 11; ++k) {
+            L.lst[k] = off;
+            off = align16(off + bytes[k]);
+        }
     }
     L.daW = L.daW1 = L.daB = L.daW5 = L.daH = L.daHS = L.daX = L.daP = L.daF = L.daSM = 0;
     if (da) {
@@ -117,10 +137,30 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     return L;
 }
 
-size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible, int da)
+size_t engine_smem_bytes(int max_mol, int max_n, int max_m, int cluster, int resident, int any_flexible, int da,
+                         const int *lmax)
 {
     const int slice = (max_n + cluster - 1) / cluster;
-    return (size_t)smem_layout(max_mol, slice, max_m, max_n, resident, any_flexible, da, cluster).total;
+    return (size_t)smem_layout(max_mol, slice, max_m, max_n, resident, any_flexible, da, cluster, lmax).total;
+}
+
+// Static per-molecule lists (DevMol offsets index the global arrays).  Resident launches
+// read shared-memory copies of their simulation's ranges, shifted by the range starts.
+struct Lists {
+    const int2 *bonds;
+    const int4 *angles, *tors;
+    const float4 *torsV, *torsS;
+    const int2 *indsub;
+    const int4 *flexres, *flexopt;
+    const int *branch, *localres, *crankres;
+    int base[9];
+};
+
+__device__ __forceinline__ Lists global_lists(const EngineArgs &a)
+{
+    Lists Ls{a.bonds, a.angles, a.tors, a.torsV, a.torsS, a.indsub, a.flexres, a.flexopt, a.branch, a.localres,
+             a.crankres, {0, 0, 0, 0, 0, 0, 0, 0, 0}};
+    return Ls;
 }
 
 // ------------------------------------------------------------------ helpers
@@ -243,11 +283,11 @@ __device__ __forceinline__ bool intra_excluded(int4 ei, int4 ej)
 
 // One bonded term (kcal/mol) of a molecule at coordinates `p`: kind 0 bond, 1 angle,
 // 2 torsion (src/Potential.cpp:45-98 with Potential::total's factors).
-__device__ float bonded_item(const EngineArgs &a, const DevMol &mol, const float4 *p, float L, float invL, int kind,
+__device__ float bonded_item(const Lists &a, const DevMol &mol, const float4 *p, float L, float invL, int kind,
                              int k)
 {
     if (kind == 0) {  // 0.5 K (r - R0)^2, minimum-image distance
-        const int2 b = a.bonds[mol.bond_off + k];
+        const int2 b = a.bonds[mol.bond_off + k - a.base[kLBond]];
         const float4 pi = p[b.x], pj = p[b.y];
         const float dx = min_image(pj.x - pi.x, L, invL), dy = min_image(pj.y - pi.y, L, invL),
                     dz = min_image(pj.z - pi.z, L, invL);
@@ -255,7 +295,7 @@ __device__ float bonded_item(const EngineArgs &a, const DevMol &mol, const float
         return 0.5f * kKSpring * rr * rr;
     }
     if (kind == 1) {  // -(1/gamma) log(exp(-gamma(ka(t-ta)^2 + ea)) + exp(-gamma kb (t-tb)^2))
-        const int4 an = a.angles[mol.ang_off + k];
+        const int4 an = a.angles[mol.ang_off + k - a.base[kLAng]];
         const float4 pi = p[an.x], pj = p[an.y], pk = p[an.z];
         const float abx = pi.x - pj.x, aby = pi.y - pj.y, abz = pi.z - pj.z;
         const float cbx = pk.x - pj.x, cby = pk.y - pj.y, cbz = pk.z - pj.z;
@@ -269,8 +309,9 @@ __device__ float bonded_item(const EngineArgs &a, const DevMol &mol, const float
         return -kGammaAngleRecip * logf(term);
     }
     // sum_n V_n (1 + cos(n phi - sigma_n))
-    const int4 tq = a.tors[mol.tor_off + k];
-    const float4 V = a.torsV[mol.tor_off + k], Sg = a.torsS[mol.tor_off + k];
+    const int ti = mol.tor_off + k - a.base[kLTor];
+    const int4 tq = a.tors[ti];
+    const float4 V = a.torsV[ti], Sg = a.torsS[ti];
     const float4 p1 = p[tq.x], p2 = p[tq.y], p3 = p[tq.z], p4 = p[tq.w];
     const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
     const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
@@ -285,7 +326,7 @@ __device__ float bonded_item(const EngineArgs &a, const DevMol &mol, const float
 
 // Bonded terms of one molecule, one flat index over bonds, angles and torsions so that
 // each thread evaluates one term: thread-strided from t0 by `stride`.
-__device__ void bonded_terms(const EngineArgs &a, const DevMol &mol, const float4 *p, float L, float invL, int t0,
+__device__ void bonded_terms(const Lists &a, const DevMol &mol, const float4 *p, float L, float invL, int t0,
                              int stride, FF &acc)
 {
     const int nb = mol.nbond, na = mol.nang, nt = mol.ntor;
@@ -309,7 +350,7 @@ __device__ __forceinline__ T ld_state(const T *p)
 }
 
 template <bool RES>
-__device__ void decide_move(const EngineArgs &a, const DevSim &S, const DevMol *mols, const float4 *CEN,
+__device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols, const float4 *CEN,
                             const float4 *P, float tstep, float rstep, const uint32_t *w, MoveDesc &mv)
 {
     const int M = S.M;
@@ -366,12 +407,12 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, const DevMol *
         }
         const float3 u = normalized(dx, dy, dz);
         axis_angle_matrix(rstep, u.x, u.y, u.z, false, mv.R);
-        const int4 fr = a.flexres[mol.flex_off + pickw(w[5], mol.nflex)];
+        const int4 fr = a.flexres[mol.flex_off + pickw(w[5], mol.nflex) - a.base[kLFlex]];
         if (fr.y <= 0) {
             mv.null_move = 1;
             break;
         }
-        const int4 op = a.flexopt[fr.z + pickw(w[6], fr.y)];
+        const int4 op = a.flexopt[fr.z + pickw(w[6], fr.y) - a.base[kLFopt]];
         mv.ri = fr.x;
         mv.br_off = op.y;
         mv.br_cnt = op.z;
@@ -389,7 +430,7 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, const DevMol *
                 mv.null_move = 1;
                 break;
             }
-            mv.ri = a.localres[mol.local_off + pickw(w[6], mol.nlocal)];
+            mv.ri = a.localres[mol.local_off + pickw(w[6], mol.nlocal) - a.base[kLLocal]];
             const float3 u = normalized(dx, dy, dz);
             const float s = (float)((double)0.1f * (double)tstep);
             vx = u.x * s, vy = u.y * s, vz = u.z * s;
@@ -398,7 +439,7 @@ __device__ void decide_move(const EngineArgs &a, const DevSim &S, const DevMol *
                 mv.null_move = 1;
                 break;
             }
-            const int ri = a.crankres[mol.crank_off + pickw(w[6], mol.ncrank)];
+            const int ri = a.crankres[mol.crank_off + pickw(w[6], mol.ncrank) - a.base[kLCrank]];
             if (ri < 1 || ri + 1 >= mv.n) {  // needs both backbone neighbours in the array
                 mv.null_move = 1;
                 break;
@@ -495,7 +536,8 @@ __device__ void da_load_weights(const EngineArgs &a, DaView &v, int rank, int t,
     }
     for (int c = t; c < S; c += T)
         v.W5[c] = a.sur_P[kOffW5 + c0 + c];
-    v.b5 = a.sur_P[kOffB5];
+    if (t == 0)
+        v.b5 = a.sur_P[kOffB5];
 }
 
 // Predictions F[0..R) of the pose rows X[0..R) (R <= RP).  Every CTA of the cluster
@@ -676,6 +718,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     __shared__ double s_ds;        // delayed acceptance: surrogate energy change of the proposal
     __shared__ int s_skip;         // ... 1 when stage 1 rejected it
     __shared__ DAStats s_da;
+    __shared__ Lists s_lists;      // static-list views (shared: keeps them out of registers)
+    __shared__ DaView s_dv;
 
     const int C = a.cluster;
     const int t = threadIdx.x, T = blockDim.x, lane = t & 31, warp = t >> 5, NW = T >> 5;
@@ -694,7 +738,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     const int r = g - S.rep_off;
     const int N = S.N, M = S.M;
     const int slice = (a.max_n + C - 1) / C;
-    const SmemLayout Ly = smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible, DA ? 1 : 0, C);
+    const SmemLayout Ly =
+        smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible, DA ? 1 : 0, C, a.lmax);
     // screening is on for this simulation (uniform over the cluster: one simulation)
     const bool da_on = DA && a.sim_da[s] != 0;
     float *s_table = reinterpret_cast<float *>(smem + Ly.table);
@@ -770,11 +815,55 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     unsigned long long pairs = 0;
     unsigned errbits = 0;
     if (t == 0)
+        s_lists = global_lists(a);
+    if (RES && a.any_flexible) {
+        // this simulation's static lists into shared memory
+        int2 *lb = reinterpret_cast<int2 *>(smem + Ly.lst[0]);
+        int4 *la = reinterpret_cast<int4 *>(smem + Ly.lst[1]);
+        int4 *lt = reinterpret_cast<int4 *>(smem + Ly.lst[2]);
+        float4 *ltv = reinterpret_cast<float4 *>(smem + Ly.lst[3]);
+        float4 *lts = reinterpret_cast<float4 *>(smem + Ly.lst[4]);
+        int2 *li = reinterpret_cast<int2 *>(smem + Ly.lst[5]);
+        int4 *lf = reinterpret_cast<int4 *>(smem + Ly.lst[6]);
+        int4 *lfo = reinterpret_cast<int4 *>(smem + Ly.lst[7]);
+        int *lbr = reinterpret_cast<int *>(smem + Ly.lst[8]);
+        int *ll = reinterpret_cast<int *>(smem + Ly.lst[9]);
+        int *lc = reinterpret_cast<int *>(smem + Ly.lst[10]);
+        const int *B = S.lbase, *Nn = S.lcount;
+        for (int k = t; k < Nn[kLBond]; k += T)
+            lb[k] = a.bonds[B[kLBond] + k];
+        for (int k = t; k < Nn[kLAng]; k += T)
+            la[k] = a.angles[B[kLAng] + k];
+        for (int k = t; k < Nn[kLTor]; k += T) {
+            lt[k] = a.tors[B[kLTor] + k];
+            ltv[k] = a.torsV[B[kLTor] + k];
+            lts[k] = a.torsS[B[kLTor] + k];
+        }
+        for (int k = t; k < Nn[kLInd]; k += T)
+            li[k] = a.indsub[B[kLInd] + k];
+        for (int k = t; k < Nn[kLFlex]; k += T)
+            lf[k] = a.flexres[B[kLFlex] + k];
+        for (int k = t; k < Nn[kLFopt]; k += T)
+            lfo[k] = a.flexopt[B[kLFopt] + k];
+        for (int k = t; k < Nn[kLBranch]; k += T)
+            lbr[k] = a.branch[B[kLBranch] + k];
+        for (int k = t; k < Nn[kLLocal]; k += T)
+            ll[k] = a.localres[B[kLLocal] + k];
+        for (int k = t; k < Nn[kLCrank]; k += T)
+            lc[k] = a.crankres[B[kLCrank] + k];
+        if (t == 0)
+            s_lists = Lists{lb, la, lt, ltv, lts, li, lf, lfo, lbr, ll, lc,
+                            {B[0], B[1], B[2], B[3], B[4], B[5], B[6], B[7], B[8]}};
+    }
+    const Lists &Ls = s_lists;
+    if (t == 0)
         s_pot = __ldcg(&a.potential[g]);
     __syncthreads();
-    DaView dv;
+    DaView &dv = s_dv;
     if (DA) {
-        dv = da_view(smem, Ly, C, a.max_m);
+        if (t == 0)
+            dv = da_view(smem, Ly, C, a.max_m);
+        __syncthreads();
         if (da_on) {
             da_load_weights(a, dv, rank, t, T);
             __syncthreads();
@@ -800,7 +889,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 for (int k = 0; k < 4; ++k)
                     w[4 * b + k] = __shfl_sync(0xffffffffu, o[k], b);
             if (lane == 0) {
-                decide_move<RES>(a, S, s_mols, CEN, P, tstep, rstep, w, mv);
+                decide_move<RES>(Ls, S, s_mols, CEN, P, tstep, rstep, w, mv);
                 s_old_row = RES ? ROWSUM[mv.m] : 0.0;
             }
         }
@@ -890,7 +979,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         if (type == kFlex && !nullm) {
             // rotate the branch about the pivot, accumulate the displacement
             for (int k = t; k < mv.br_cnt; k += T) {
-                const int i = a.branch[mv.br_off + k];
+                const int i = Ls.branch[mv.br_off + k - Ls.base[kLBranch]];
                 const float4 p = s_ipos[i];
                 const float3 rr = rot_apply(mv.R, p.x - mv.px, p.y - mv.py, p.z - mv.pz);
                 s_disp[i] = make_float4((rr.x + mv.px) - p.x, (rr.y + mv.py) - p.y, (rr.z + mv.pz) - p.z, 0.f);
@@ -1005,19 +1094,24 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 }
                 ff_add(iacc, part);
             }
-            if (rank == 0) {
+            {
+                // indirect neighbours not caught by the rules above, and the bonded terms,
+                // spread over every thread of the cluster
                 const DevMol &mol = s_mols[m];
-                // indirect neighbours not caught by the rules above
-                for (int k = t; k < mol.nind; k += T) {
-                    const int2 pr = a.indsub[mol.ind_off + k];
+                for (int k = rank * T + t; k < mol.nind; k += C * T) {
+                    const int2 pr = Ls.indsub[mol.ind_off + k - Ls.base[kLInd]];
                     ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
                 }
-                bonded_terms(a, mol, s_ipos, L, invL, t, T, iacc);
+                bonded_terms(Ls, mol, s_ipos, L, invL, rank * T + t, C * T, iacc);
             }
         }
         __syncthreads();
 
-        // ---- per-molecule partial rows of this CTA's slice (float-float, then double)
+        // ---- per-molecule partial rows of this CTA's slice (float-float, then double).
+        // In a cluster every CTA pushes its partials into every CTA's receive slots
+        // (step parity, source rank) before the barrier, so nothing is read remotely after it.
+        const int M1 = a.max_m + 1;
+        double *rcv = reinterpret_cast<double *>(smem + Ly.rcv) + (step & 1) * C * M1;
         for (int b = warp; b < M; b += NW) {
             FF acc{0.f, 0.f};
             if (b != m) {
@@ -1030,33 +1124,42 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 }
                 acc = ff_warp_sum(acc);
             }
-            if (lane == 0)
-                s_rowp[b] = (b != m) ? ff_value(acc) : 0.0;
+            // lane 0's value for every receiver (lanes may differ in the low word)
+            const double v = __shfl_sync(0xffffffffu, (b != m) ? ff_value(acc) : 0.0, 0);
+            if (C > 1) {
+                if (lane < C)
+                    cg::this_cluster().map_shared_rank(rcv, lane)[rank * M1 + b] = v;
+            } else if (lane == 0) {
+                s_rowp[b] = v;
+            }
         }
         if (flexmol) {
             const double v = block_sum_ff(iacc, s_red);
-            if (t == 0)
+            if (C > 1) {
+                if (t < C)
+                    cg::this_cluster().map_shared_rank(rcv, t)[rank * M1 + a.max_m] = v;
+            } else if (t == 0) {
                 s_intrap = v;
+            }
         }
         if (C > 1)
             cg::this_cluster().sync();
         else
             __syncthreads();
 
-        // ---- gather the cluster's partials (fixed rank order), Metropolis
+        // ---- sum the cluster's partials (fixed rank order, local reads), Metropolis
         if (C > 1) {
-            cg::cluster_group cl = cg::this_cluster();
             for (int b = t; b < M; b += T) {
                 double v = 0.0;
                 for (int k = 0; k < C; ++k)
-                    v += cl.map_shared_rank(s_rowp, k)[b];
+                    v += rcv[k * M1 + b];
                 s_row[b] = v;
             }
             if (t == 0) {
                 double v = 0.0;
                 if (flexmol)
                     for (int k = 0; k < C; ++k)
-                        v += *cl.map_shared_rank(&s_intrap, k);
+                        v += rcv[k * M1 + a.max_m];
                 s_intra_new = v;
             }
             __syncthreads();
@@ -1176,11 +1279,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 }
             }
         }
-        if (C > 1)
+        // Resident CTAs own their state copies and every cross-CTA value of a step
+        // travels through the receive slots (double-buffered by step parity), so a CTA
+        // barrier suffices; without residency rank 0's global commit must be visible
+        // to the cluster before the next step reads it.
+        if (C > 1 && !RES)
             cg::this_cluster().sync();
         else
             __syncthreads();
     }
+    if (C > 1)  // no CTA leaves while another may still read its shared memory
+        cg::this_cluster().sync();
 
     // ---- write back (rank 0)
     if (rank == 0) {
@@ -1293,7 +1402,7 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
             const int2 pr = a.indsub[mol.ind_off + k];
             ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
         }
-        bonded_terms(a, mol, s_ipos, L, invL, t, T, iacc);
+        bonded_terms(global_lists(a), mol, s_ipos, L, invL, t, T, iacc);
     }
     const double v = block_sum_ff(iacc, s_red);
     if (t == 0)

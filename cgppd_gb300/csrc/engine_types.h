@@ -46,6 +46,10 @@ struct DevSim {
     unsigned long long thr4[4];  // cumulative weights, flexible molecule
     unsigned long long thr3[3];  // cumulative weights, only molecule
     unsigned long long thr_rot;  // rigid molecule: rotate below, translate above
+    // this simulation's ranges of the static lists (first index, count): bonds, angles,
+    // torsions (+ their V / phase), indirect pairs, flex residues, flex options, branch
+    // residues, local residues, crankshaft residues
+    int lbase[9], lcount[9];
 };
 
 struct DevMol {
@@ -128,6 +132,7 @@ struct EngineArgs {
     int max_n;                   // largest N
     int max_m;                   // largest M
     int max_mol;                 // largest molecule
+    int lmax[9];                 // largest per-simulation count of each static list
     // delayed acceptance with the learned surrogate (da != 0: k_mc<.., true> is launched)
     int da;
     const float *sur_P;          // FP32 master parameters
