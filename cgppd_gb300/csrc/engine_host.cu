@@ -577,7 +577,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     base.potential = pot.ptr, base.stats = st.ptr, base.stepc = sc.ptr, base.pairc = pc.ptr, base.errflags = ef.ptr;
     if (e->da)
         base.dastats = das.ptr;
-    const int clusters[4] = {1, 2, 4, 8}, thread_opts[2] = {128, 256};
+    const int clusters[5] = {1, 2, 4, 8, 16}, thread_opts[3] = {128, 256, 512};
     const int steps = 32;
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
@@ -735,7 +735,8 @@ int cgppd_engine_finalize(cgppd_engine *e, int cluster, int threads)
     if (e->build() != 0)
         return -1;
     const bool tune = cluster <= 0 || threads <= 0;
-    configure_shape(e, std::min(8, std::max(1, cluster > 0 ? cluster : 1)), threads == 128 ? 128 : 256);
+    configure_shape(e, std::min(16, std::max(1, cluster > 0 ? cluster : 1)),
+                    threads == 128 ? 128 : threads == 512 ? 512 : 256);
     const size_t s_init = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, 1, 0, e->any_flexible, 0, nullptr);
     if (std::max(e->smem, s_init) > 227 * 1024)
         return cgppd_fail("cgppd_engine_finalize: system too large for shared memory (reduce molecule size or N)");

@@ -39,7 +39,7 @@ namespace cg = cooperative_groups;
 namespace cgppd {
 
 constexpr int kTableStride = 32;
-constexpr int kMaxThreads = 256;
+constexpr int kMaxThreads = 512;
 constexpr int kMaxWarps = kMaxThreads / 32;
 
 struct MoveDesc {
@@ -1039,27 +1039,44 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             while (tpj < 32 && cnt * tpj * 2 <= T)
                 tpj <<= 1;
         const int sub = t & (tpj - 1), jl = t / tpj, jstride = T / tpj;
+        // residue record of this thread's next j, loaded one iteration ahead
+        float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
+        if (jl < cnt) {
+            const int o = o0 + jl, j = (o < start) ? o : o + n;
+            npj = ld_state<RES>(&P[j]);
+            nsj = ST[j];
+        }
         for (int base = 0; base < cnt; base += jstride) {
             const int o = o0 + base + jl;
             const bool valid = (base + jl) < cnt;
+            const float4 pj = npj, sj = nsj;
+            if (base + jstride + jl < cnt) {
+                const int on = o + jstride, jn = (on < start) ? on : on + n;
+                npj = ld_state<RES>(&P[jn]);
+                nsj = ST[jn];
+            }
             FF acc{0.f, 0.f};
             if (valid) {
-                const int j = (o < start) ? o : o + n;
-                const float4 pj = ld_state<RES>(&P[j]);
-                const float4 sj = ST[j];
                 const float4 rj = make_float4(pj.x, pj.y, pj.z, sj.x);
                 const float2 qj = make_float2(sj.y, sj.z);
-                float part = 0.f;
-                int cntp = 0;
-                for (int i = sub; i < n; i += tpj) {
-                    part += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
-                    if (++cntp == 32) {
-                        ff_add(acc, part);
-                        part = 0.f;
+                // four independent partial sums (instruction-level parallelism), folded
+                // into the float-float accumulator every 32 terms
+                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+                int i = sub, cntp = 0;
+                for (; i + 3 * tpj < n; i += 4 * tpj) {
+                    p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                    p1 += pair_kcal(s_ipos[i + tpj], s_iq[i + tpj], rj, qj, s_table, L, invL);
+                    p2 += pair_kcal(s_ipos[i + 2 * tpj], s_iq[i + 2 * tpj], rj, qj, s_table, L, invL);
+                    p3 += pair_kcal(s_ipos[i + 3 * tpj], s_iq[i + 3 * tpj], rj, qj, s_table, L, invL);
+                    if (++cntp == 8) {
+                        ff_add(acc, (p0 + p1) + (p2 + p3));
+                        p0 = p1 = p2 = p3 = 0.f;
                         cntp = 0;
                     }
                 }
-                ff_add(acc, part);
+                for (; i < n; i += tpj)
+                    p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                ff_add(acc, (p0 + p1) + (p2 + p3));
             }
             for (int o2 = 1; o2 < tpj; o2 <<= 1) {
                 FF w{__shfl_xor_sync(0xffffffffu, acc.hi, o2), __shfl_xor_sync(0xffffffffu, acc.lo, o2)};
@@ -1072,10 +1089,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         // ---- internal energy of a flexible molecule (intra pairs split over the cluster)
         FF iacc{0.f, 0.f};
         if (flexmol) {
+            // 32 x 32 tiles on and above the diagonal; when the cluster has spare warps,
+            // each tile's i range is split into sf chunks (shorter serial chains)
             const int nt = (n + 31) >> 5;
             const int ntiles = nt * (nt + 1) / 2;
-            for (int k = rank * NW + warp; k < ntiles; k += C * NW) {
-                int ta = 0, rem = k;
+            int sf = 1;
+            while (sf < 4 && ntiles * sf * 2 <= C * NW)
+                sf <<= 1;
+            const int il = 32 / sf;
+            for (int k = rank * NW + warp; k < ntiles * sf; k += C * NW) {
+                const int tk = k / sf, ck = k - tk * sf;
+                int ta = 0, rem = tk;
                 while (rem >= nt - ta) {
                     rem -= nt - ta;
                     ++ta;
@@ -1087,10 +1111,26 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     const float4 pj = s_ipos[j];
                     const float2 qj = s_iq[j];
                     const int4 ej = s_iexcl[j];
-                    const int iend = (ta == tb) ? j : min(n, ta * 32 + 32);
-                    for (int i = ta * 32; i < iend; ++i)
-                        if (!intra_excluded(s_iexcl[i], ej))
-                            part += pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
+                    const int ib = ta * 32 + ck * il;
+                    const int iend = min((ta == tb) ? j : n, ib + il);
+                    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+                    int i = ib;
+                    // excluded pairs are evaluated and dropped (select, no divergence)
+                    for (; i + 3 < iend; i += 4) {
+                        const float e0 = pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
+                        const float e1 = pair_kcal(s_ipos[i + 1], s_iq[i + 1], pj, qj, s_table, L, invL);
+                        const float e2 = pair_kcal(s_ipos[i + 2], s_iq[i + 2], pj, qj, s_table, L, invL);
+                        const float e3 = pair_kcal(s_ipos[i + 3], s_iq[i + 3], pj, qj, s_table, L, invL);
+                        p0 += intra_excluded(s_iexcl[i], ej) ? 0.f : e0;
+                        p1 += intra_excluded(s_iexcl[i + 1], ej) ? 0.f : e1;
+                        p2 += intra_excluded(s_iexcl[i + 2], ej) ? 0.f : e2;
+                        p3 += intra_excluded(s_iexcl[i + 3], ej) ? 0.f : e3;
+                    }
+                    for (; i < iend; ++i) {
+                        const float e0 = pair_kcal(s_ipos[i], s_iq[i], pj, qj, s_table, L, invL);
+                        p0 += intra_excluded(s_iexcl[i], ej) ? 0.f : e0;
+                    }
+                    part = (p0 + p1) + (p2 + p3);
                 }
                 ff_add(iacc, part);
             }
@@ -1658,6 +1698,21 @@ cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = (C > 1) ? 1 : 0;
+    if (C > 8) {  // 16-CTA clusters are a non-portable size: opt in once per kernel
+        static bool allowed = false;
+        if (!allowed) {
+            cudaError_t e = cudaFuncSetAttribute(k_mc<true, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_mc<false, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_mc<true, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_mc<false, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e != cudaSuccess)
+                return e;
+            allowed = true;
+        }
+    }
     if (a.da) {
         if (a.resident)
             return cudaLaunchKernelEx(&cfg, k_mc<true, true>, a, nsteps);
