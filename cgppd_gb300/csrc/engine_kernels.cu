@@ -918,7 +918,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 int pass = 1;
                 if (!(dsf < 0.0f)) {
                     const float boltz = expf(-(dsf * kKcal) / (kRgas * temperature));
-                    pass = ((double)mv.w_stage1 < (double)boltz * 4294967296.0) ? 1 : 0;
+                    const unsigned long long thr = (unsigned long long)ceilf(boltz * 4294967296.0f);
+                    pass = ((unsigned long long)mv.w_stage1 < thr) ? 1 : 0;
                 }
                 s_skip = !pass;
                 s_da.proposals++;
@@ -1135,14 +1136,22 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 ff_add(iacc, part);
             }
             {
-                // indirect neighbours not caught by the rules above, and the bonded terms,
-                // spread over every thread of the cluster
+                // indirect neighbours not caught by the rules above, and the bonded terms:
+                // on the cluster's warps that hold no tile task when there are any (so
+                // no warp carries both), else over every thread
                 const DevMol &mol = s_mols[m];
-                for (int k = rank * T + t; k < mol.nind; k += C * T) {
+                const int gw = rank * NW + warp, ntask = ntiles * sf, nwarps = C * NW;
+                int b0 = rank * T + t, bstride = C * T;
+                if (ntask < nwarps) {
+                    b0 = (gw >= ntask) ? (gw - ntask) * 32 + lane : 0x7fffffff;
+                    bstride = (nwarps - ntask) * 32;
+                }
+                for (int k = b0; k < mol.nind; k += bstride) {
                     const int2 pr = Ls.indsub[mol.ind_off + k - Ls.base[kLInd]];
                     ff_add(iacc, -pair_kcal(s_ipos[pr.x], s_iq[pr.x], s_ipos[pr.y], s_iq[pr.y], s_table, L, invL));
                 }
-                bonded_terms(Ls, mol, s_ipos, L, invL, rank * T + t, C * T, iacc);
+                if (b0 != 0x7fffffff)
+                    bonded_terms(Ls, mol, s_ipos, L, invL, b0, bstride, iacc);
             }
         }
         __syncthreads();
@@ -1187,51 +1196,56 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         else
             __syncthreads();
 
-        // ---- sum the cluster's partials (fixed rank order, local reads), Metropolis
-        if (C > 1) {
-            for (int b = t; b < M; b += T) {
-                double v = 0.0;
-                for (int k = 0; k < C; ++k)
-                    v += rcv[k * M1 + b];
-                s_row[b] = v;
-            }
-            if (t == 0) {
-                double v = 0.0;
-                if (flexmol)
-                    for (int k = 0; k < C; ++k)
-                        v += rcv[k * M1 + a.max_m];
-                s_intra_new = v;
-            }
-            __syncthreads();
-        } else {
-            if (t == 0)
-                s_intra_new = flexmol ? s_intrap : 0.0;
-        }
+        // ---- sum the cluster's partials (fixed rank order, local reads) and take the
+        // Metropolis decision, all in warp 0 (no CTA barrier before the decision)
         const double *rowv = (C > 1) ? s_row : s_rowp;
         if (warp == 0) {
             double v = 0.0;
-            for (int b = lane; b < M; b += 32)
+            for (int b = lane; b < M; b += 32) {
+                double rb;
+                if (C > 1) {
+                    rb = 0.0;
+                    for (int k = 0; k < C; ++k)
+                        rb += rcv[k * M1 + b];
+                    s_row[b] = rb;
+                } else {
+                    rb = s_rowp[b];
+                }
                 if (b != m)
-                    v += rowv[b];
+                    v += rb;
+            }
             v = warp_sum_d(v);
             if (lane == 0) {
-                const double new_row = v + s_intra_new;
+                double intra_new = 0.0;
+                if (flexmol) {
+                    if (C > 1)
+                        for (int k = 0; k < C; ++k)
+                            intra_new += rcv[k * M1 + a.max_m];
+                    else
+                        intra_new = s_intrap;
+                }
+                s_intra_new = intra_new;
+                const double new_row = v + intra_new;
                 s_new_row = new_row;
-                const double newPotential = s_pot - s_old_row + new_row;
-                float delta = (float)(newPotential - s_pot);
+                const double dE = new_row - s_old_row;  // = newPotential - oldPotential
+                float delta = (float)dE;
                 if (DA && screened)  // stage 2: exact change less the surrogate's
-                    delta = (float)((newPotential - s_pot) - s_ds);
+                    delta = (float)(dE - s_ds);
                 int acc = 0;
                 if (delta < 0.0f) {
                     acc = 1;
                 } else {
+                    // u = w / 2^32 < boltz  <=>  w < boltz 2^32, exact in float (power-of-two
+                    // scaling) and compared as integers
                     const float boltz = expf(-(delta * kKcal) / (kRgas * temperature));
-                    acc = ((double)mv.w_metro < (double)boltz * 4294967296.0) ? 2 : 0;
+                    const unsigned long long thr = (unsigned long long)ceilf(boltz * 4294967296.0f);
+                    acc = ((unsigned long long)mv.w_metro < thr) ? 2 : 0;
                 }
-                if (!isfinite(newPotential))
+                if (!isfinite(dE))
                     acc = 0;
+                const double newPotential = s_pot - s_old_row + new_row;
                 if (DA && screened) {
-                    const double dE = newPotential - s_pot, e = dE - s_ds;
+                    const double e = dE - s_ds;
                     s_da.stage2_eval++;
                     if (acc)
                         s_da.stage2_accept++;
