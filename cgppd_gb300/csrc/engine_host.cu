@@ -126,7 +126,7 @@ struct cgppd_engine {
     size_t smem = 0;
     int total_replicas = 0;
     int max_n = 0, max_m = 0, max_mol = 0;
-    int lmax[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // largest per-simulation static list sizes
+    int lmax[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // largest per-simulation static list sizes
     int resident = 0, any_flexible = 0;
     int resident_pref = 1;
     // delayed acceptance
@@ -153,6 +153,7 @@ struct cgppd_engine {
     DevBuf<int4> d_angles, d_tors, d_flexres, d_flexopt;
     DevBuf<float4> d_torsV, d_torsS;
     DevBuf<int> d_branch, d_localres, d_crankres;
+    DevBuf<int2> d_tiles;
     DevBuf<float> d_table;
     DevBuf<float4> d_pos, d_rel, d_center;
     DevBuf<double> d_emat, d_intra, d_potential, d_scratch_pot, d_scratch_emat, d_scratch_intra;
@@ -201,6 +202,7 @@ struct cgppd_engine {
         a.branch = d_branch.ptr;
         a.localres = d_localres.ptr;
         a.crankres = d_crankres.ptr;
+        a.tiles = d_tiles.ptr;
         a.table = d_table.ptr;
         a.pos = d_pos.ptr;
         a.rel = d_rel.ptr;
@@ -229,7 +231,7 @@ struct cgppd_engine {
         a.max_n = max_n;
         a.max_m = max_m;
         a.max_mol = max_mol;
-        for (int k = 0; k < 9; ++k)
+        for (int k = 0; k < 10; ++k)
             a.lmax[k] = lmax[k];
         a.resident = resident;
         a.any_flexible = any_flexible;
@@ -252,7 +254,7 @@ int cgppd_engine::build()
 {
     std::vector<float4> rstat;
     std::vector<int4> rexcl, angles, tors, flexres, flexopt;
-    std::vector<int2> bonds, indsub;
+    std::vector<int2> bonds, indsub, tiles;
     std::vector<float4> torsVv, torsSv;
     std::vector<int> branch, localres, crankres, rep_sim;
     std::vector<float4> pos, rel, center;
@@ -308,7 +310,7 @@ int cgppd_engine::build()
         auto list_sizes = [&]() {
             return std::vector<int>{(int)bonds.size(), (int)angles.size(), (int)tors.size(), (int)indsub.size(),
                                     (int)flexres.size(), (int)flexopt.size(), (int)branch.size(),
-                                    (int)localres.size(), (int)crankres.size()};
+                                    (int)localres.size(), (int)crankres.size(), (int)tiles.size()};
         };
         const std::vector<int> lbase = list_sizes();
         // replica-wide UIDs (Graph::assign_uids with running offsets, src/Replica.cpp:33-40)
@@ -405,6 +407,22 @@ int cgppd_engine::build()
                         if (!excluded(i, j) && !G.indirect_neighbours.count(Pair{i, j}))
                             ++nintra;
                 dm.nintra = (int)nintra;
+                // 32 x 32 tiles (ta <= tb) with at least one pair i < j that the rules keep
+                dm.tile_off = (int)tiles.size();
+                const int nt = (hm.n + 31) / 32;
+                for (int ta = 0; ta < nt; ++ta)
+                    for (int tb = ta; tb < nt; ++tb) {
+                        bool any = false;
+                        for (int i = ta * 32; i < std::min(hm.n, ta * 32 + 32) && !any; ++i)
+                            for (int j = std::max(i + 1, tb * 32); j < std::min(hm.n, tb * 32 + 32); ++j)
+                                if (!excluded(i, j)) {
+                                    any = true;
+                                    break;
+                                }
+                        if (any)
+                            tiles.push_back(make_int2(ta, tb));
+                    }
+                dm.ntile = (int)tiles.size() - dm.tile_off;
                 // flex candidates: branch of each (residue, neighbour) edge, extended by the
                 // other branches inside the residue's rigid domain (src/Molecule.cpp:331-360)
                 dm.flex_off = (int)flexres.size();
@@ -437,7 +455,7 @@ int cgppd_engine::build()
             max_mol = std::max(max_mol, hm.n);
         }
         const std::vector<int> lend = list_sizes();
-        for (int k = 0; k < 9; ++k) {
+        for (int k = 0; k < 10; ++k) {
             ds.lbase[k] = lbase[k];
             ds.lcount[k] = lend[k] - lbase[k];
             lmax[k] = std::max(lmax[k], ds.lcount[k]);
@@ -501,6 +519,7 @@ int cgppd_engine::build()
     rc |= d_branch.upload(branch);
     rc |= d_localres.upload(localres);
     rc |= d_crankres.upload(crankres);
+    rc |= d_tiles.upload(tiles);
     rc |= d_table.upload(table);
     rc |= d_pos.upload(pos);
     rc |= d_rel.upload(rel);

@@ -59,7 +59,7 @@ struct MoveDesc {
 struct SmemLayout {
     int table, mols, ipos, irel, iexcl, idisp, iq, ej, rowp, row;    // always
     int rcv;                                                         // clusters: pushed partial rows
-    int lst[11];                                                     // resident + flexible: static lists
+    int lst[12];                                                     // resident + flexible: static lists
     int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM;                        // resident only
     int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
     int total;
@@ -75,7 +75,8 @@ __host__ __device__ inline int da_rows(int max_m) { return (((max_m - 1 > 1 ? ma
 
 __host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
 
-enum ListId { kLBond = 0, kLAng, kLTor, kLInd, kLFlex, kLFopt, kLBranch, kLLocal, kLCrank };
+enum ListId { kLBond = 0, kLAng, kLTor, kLInd, kLFlex, kLFopt, kLBranch, kLLocal, kLCrank, kLTile };
+constexpr int kNumLists = 10;
 
 __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int max_m, int max_n, int resident,
                                                   int any_flexible, int da = 0, int C = 1,
@@ -106,15 +107,15 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
         L.INTRA = off;  off = align16(off + 8 * max_m);
         L.ROWSUM = off; off = align16(off + 8 * max_m);
     }
-    for (int k = 0; k < 11; ++k)
+    for (int k = 0; k < 12; ++k)
         L.lst[k] = 0;
     if (resident && any_flexible && lmax) {
         // bonds, angles, torsions, torsion V, torsion phases, indirect pairs, flex residues,
-        // flex options, branch residues, local residues, crankshaft residues
-        const int bytes[11] = {8 * lmax[kLBond], 16 * lmax[kLAng], 16 * lmax[kLTor], 16 * lmax[kLTor],
+        // flex options, branch residues, local residues, crankshaft residues, intra tiles
+        const int bytes[12] = {8 * lmax[kLBond], 16 * lmax[kLAng], 16 * lmax[kLTor], 16 * lmax[kLTor],
                                16 * lmax[kLTor], 8 * lmax[kLInd], 16 * lmax[kLFlex], 16 * lmax[kLFopt],
-                               4 * lmax[kLBranch], 4 * lmax[kLLocal], 4 * lmax[kLCrank]};
-        for (int k = 0; k < 11; ++k) {
+                               4 * lmax[kLBranch], 4 * lmax[kLLocal], 4 * lmax[kLCrank], 8 * lmax[kLTile]};
+        for (int k = 0; k < 12; ++k) {
             L.lst[k] = off;
             off = align16(off + bytes[k]);
         }
@@ -153,13 +154,14 @@ struct Lists {
     const int2 *indsub;
     const int4 *flexres, *flexopt;
     const int *branch, *localres, *crankres;
-    int base[9];
+    const int2 *tiles;
+    int base[kNumLists];
 };
 
 __device__ __forceinline__ Lists global_lists(const EngineArgs &a)
 {
     Lists Ls{a.bonds, a.angles, a.tors, a.torsV, a.torsS, a.indsub, a.flexres, a.flexopt, a.branch, a.localres,
-             a.crankres, {0, 0, 0, 0, 0, 0, 0, 0, 0}};
+             a.crankres, a.tiles, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
     return Ls;
 }
 
@@ -215,10 +217,10 @@ __device__ __forceinline__ float3 rot_apply(const float *R, float x, float y, fl
 
 // Rotation matrix of the quaternion (cos(a/2), sin(a/2) axis) (src/Quaternion.cpp:12-21,
 // :95-112), optionally normalised first (Quaternion::normalize, :30-38).
-__device__ void axis_angle_matrix(float angle, float ax, float ay, float az, bool normalize, float *R)
+// Rotation matrix of the quaternion (cos(angle/2), sin(angle/2) * axis); (s, c) are
+// sin/cos of angle/2 (precomputed per launch for the replica's fixed step angle).
+__device__ void axis_angle_matrix_sc(float s, float c, float ax, float ay, float az, bool normalize, float *R)
 {
-    float s, c;
-    sincosf(0.5f * angle, &s, &c);
     float w = c, x = s * ax, y = s * ay, z = s * az;
     if (normalize) {
         const float inv = 1.0f / sqrtf(w * w + x * x + y * y + z * z);
@@ -237,8 +239,26 @@ __device__ void axis_angle_matrix(float angle, float ax, float ay, float az, boo
     R[8] = w2 - x2 - y2 + z2;
 }
 
-// Molecule::wrapped_centre: fmod per component (keeps the sign).
-__device__ __forceinline__ float wrapf(float c, float box) { return fmodf(c, box); }
+__device__ void axis_angle_matrix(float angle, float ax, float ay, float az, bool normalize, float *R)
+{
+    float s, c;
+    sincosf(0.5f * angle, &s, &c);
+    axis_angle_matrix_sc(s, c, ax, ay, az, normalize, R);
+}
+
+// Molecule::wrapped_centre: fmod per component (keeps the sign).  Centres move by a few
+// A per step, so |c| < 2 box: then fmod is c, c - box or c + box, each exact (Sterbenz);
+// c == -box (fmod gives -0) and larger |c| take fmodf itself.
+__device__ __forceinline__ float wrapf(float c, float box)
+{
+    if (fabsf(c) < box)
+        return c;
+    if (c >= box && c < 2.0f * box)
+        return c - box;
+    if (c < -box && c > -2.0f * box)
+        return c + box;
+    return fmodf(c, box);
+}
 
 // floor(u * n) for u = w / 2^32, exactly.
 __device__ __forceinline__ int pickw(uint32_t w, int n) { return (int)(((unsigned long long)w * (unsigned)n) >> 32); }
@@ -351,7 +371,8 @@ __device__ __forceinline__ T ld_state(const T *p)
 
 template <bool RES>
 __device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols, const float4 *CEN,
-                            const float4 *P, float tstep, float rstep, const uint32_t *w, MoveDesc &mv)
+                            const float4 *P, float tstep, float rstep, const float4 rsc, const uint32_t *w,
+                            MoveDesc &mv)
 {
     const int M = S.M;
     mv.m = pickw(w[0], M);
@@ -396,7 +417,7 @@ __device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols,
     case kRotate: {
         // Molecule::rotate(rng, step) -> setRotation (src/Molecule.cpp:193-208, :255-260)
         const float3 u = normalized(dx, dy, dz);
-        axis_angle_matrix(rstep, u.x, u.y, u.z, true, mv.R);
+        axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, true, mv.R);
         break;
     }
     case kFlex: {
@@ -406,7 +427,7 @@ __device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols,
             break;
         }
         const float3 u = normalized(dx, dy, dz);
-        axis_angle_matrix(rstep, u.x, u.y, u.z, false, mv.R);
+        axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, false, mv.R);
         const int4 fr = a.flexres[mol.flex_off + pickw(w[5], mol.nflex) - a.base[kLFlex]];
         if (fr.y <= 0) {
             mv.null_move = 1;
@@ -451,7 +472,7 @@ __device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols,
             const float4 pp = ld_state<RES>(&Pm[ri + 1]);
             const float3 ax = normalized(pp.x - pm.x, pp.y - pm.y, pp.z - pm.z);
             float Rm[9];
-            axis_angle_matrix(flip ? -rstep : rstep, ax.x, ax.y, ax.z, true, Rm);
+            axis_angle_matrix_sc(flip ? rsc.z : rsc.x, flip ? rsc.w : rsc.y, ax.x, ax.y, ax.z, true, Rm);
             const float3 rr = rot_apply(Rm, p0.x - pm.x, p0.y - pm.y, p0.z - pm.z);
             vx = (rr.x + pm.x) - p0.x;
             vy = (rr.y + pm.y) - p0.y;
@@ -719,6 +740,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     __shared__ int s_skip;         // ... 1 when stage 1 rejected it
     __shared__ DAStats s_da;
     __shared__ Lists s_lists;      // static-list views (shared: keeps them out of registers)
+    __shared__ uint32_t s_w[12];   // the next step's Philox words, drawn one step ahead
     __shared__ DaView s_dv;
 
     const int C = a.cluster;
@@ -811,6 +833,21 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     const float temperature = a.temperature[g];
     const uint32_t key0 = a.seed_lo ^ (0x9E3779B9u * (uint32_t)(g + 1)), key1 = a.seed_hi;
     const unsigned long long step0 = a.stepc[g];
+    // sin/cos of +-rstep/2, the replica's fixed rotation half-angles
+    float4 rsc;
+    sincosf(0.5f * rstep, &rsc.x, &rsc.y);
+    sincosf(-(0.5f * rstep), &rsc.z, &rsc.w);
+    // Philox words of step mcstep (counter (step, step_hi, lane, 'MC')), lanes 0-2 of a warp
+    auto draw = [&](unsigned long long mcstep) {
+        if (lane < 3) {
+            const U4 ctr{(uint32_t)mcstep, (uint32_t)(mcstep >> 32), (uint32_t)lane, 0x4D43u};
+            const U4 res = philox4x32_10(ctr, key0, key1);
+            s_w[4 * lane + 0] = res.x, s_w[4 * lane + 1] = res.y, s_w[4 * lane + 2] = res.z,
+                           s_w[4 * lane + 3] = res.w;
+        }
+    };
+    if (warp == 0)
+        draw(step0);
     // pair and error counters live in registers of thread 0 (rank 0 writes them back)
     unsigned long long pairs = 0;
     unsigned errbits = 0;
@@ -829,6 +866,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         int *lbr = reinterpret_cast<int *>(smem + Ly.lst[8]);
         int *ll = reinterpret_cast<int *>(smem + Ly.lst[9]);
         int *lc = reinterpret_cast<int *>(smem + Ly.lst[10]);
+        int2 *ltl = reinterpret_cast<int2 *>(smem + Ly.lst[11]);
         const int *B = S.lbase, *Nn = S.lcount;
         for (int k = t; k < Nn[kLBond]; k += T)
             lb[k] = a.bonds[B[kLBond] + k];
@@ -851,9 +889,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             ll[k] = a.localres[B[kLLocal] + k];
         for (int k = t; k < Nn[kLCrank]; k += T)
             lc[k] = a.crankres[B[kLCrank] + k];
+        for (int k = t; k < Nn[kLTile]; k += T)
+            ltl[k] = a.tiles[B[kLTile] + k];
         if (t == 0)
-            s_lists = Lists{lb, la, lt, ltv, lts, li, lf, lfo, lbr, ll, lc,
-                            {B[0], B[1], B[2], B[3], B[4], B[5], B[6], B[7], B[8]}};
+            s_lists = Lists{lb, la, lt, ltv, lts, li, lf, lfo, lbr, ll, lc, ltl,
+                            {B[0], B[1], B[2], B[3], B[4], B[5], B[6], B[7], B[8], B[9]}};
     }
     const Lists &Ls = s_lists;
     if (t == 0)
@@ -874,24 +914,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 
     for (int step = 0; step < nsteps; ++step) {
         const unsigned long long mcstep = step0 + (unsigned long long)step;
-        // ---- draws (lanes 0-2 of warp 0) and the move decision (thread 0)
-        if (warp == 0) {
-            uint32_t o[4] = {0u, 0u, 0u, 0u};
-            if (lane < 3) {
-                const U4 ctr{(uint32_t)mcstep, (uint32_t)(mcstep >> 32), (uint32_t)lane, 0x4D43u};
-                const U4 res = philox4x32_10(ctr, key0, key1);
-                o[0] = res.x, o[1] = res.y, o[2] = res.z, o[3] = res.w;
-            }
+        // ---- the move decision (thread 0) from the words drawn one step ahead
+        if (t == 0) {
             uint32_t w[12];
 #pragma unroll
-            for (int b = 0; b < 3; ++b)
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    w[4 * b + k] = __shfl_sync(0xffffffffu, o[k], b);
-            if (lane == 0) {
-                decide_move<RES>(Ls, S, s_mols, CEN, P, tstep, rstep, w, mv);
-                s_old_row = RES ? ROWSUM[mv.m] : 0.0;
-            }
+            for (int k = 0; k < 12; ++k)
+                w[k] = s_w[k];
+            decide_move<RES>(Ls, S, s_mols, CEN, P, tstep, rstep, rsc, w, mv);
+            s_old_row = RES ? ROWSUM[mv.m] : 0.0;
         }
         __syncthreads();
         const int n = mv.n, start = mv.start, type = mv.type, m = mv.m;
@@ -1090,22 +1120,19 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         // ---- internal energy of a flexible molecule (intra pairs split over the cluster)
         FF iacc{0.f, 0.f};
         if (flexmol) {
-            // 32 x 32 tiles on and above the diagonal; when the cluster has spare warps,
-            // each tile's i range is split into sf chunks (shorter serial chains)
-            const int nt = (n + 31) >> 5;
-            const int ntiles = nt * (nt + 1) / 2;
+            // the molecule's active 32 x 32 tiles (on and above the diagonal, holding at least
+            // one unexcluded pair); when the cluster has spare warps each tile's i range is
+            // split into sf chunks (shorter serial chains)
+            const DevMol &mt = s_mols[m];
+            const int ntiles = mt.ntile;
             int sf = 1;
             while (sf < 4 && ntiles * sf * 2 <= C * NW)
                 sf <<= 1;
             const int il = 32 / sf;
             for (int k = rank * NW + warp; k < ntiles * sf; k += C * NW) {
                 const int tk = k / sf, ck = k - tk * sf;
-                int ta = 0, rem = tk;
-                while (rem >= nt - ta) {
-                    rem -= nt - ta;
-                    ++ta;
-                }
-                const int tb = ta + rem;
+                const int2 tl = Ls.tiles[mt.tile_off + tk - Ls.base[kLTile]];
+                const int ta = tl.x, tb = tl.y;
                 const int j = tb * 32 + lane;
                 float part = 0.f;
                 if (j < n) {
@@ -1308,6 +1335,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
         }
         }  // !skip
+        // the next step's words, by the last warp (thread 0 read this step's before the
+        // step's first barrier; the end-of-step barrier publishes these)
+        if (warp == NW - 1)
+            draw(mcstep + 1);
         // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
         const int freq = S.sample_freq;
         if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&

@@ -48,8 +48,8 @@ struct DevSim {
     unsigned long long thr_rot;  // rigid molecule: rotate below, translate above
     // this simulation's ranges of the static lists (first index, count): bonds, angles,
     // torsions (+ their V / phase), indirect pairs, flex residues, flex options, branch
-    // residues, local residues, crankshaft residues
-    int lbase[9], lcount[9];
+    // residues, local residues, crankshaft residues, active intra tiles
+    int lbase[10], lcount[10];
 };
 
 struct DevMol {
@@ -63,6 +63,7 @@ struct DevMol {
     int crank_off, ncrank;
     int nintra;                  // intra pairs that are not excluded (flexible molecules)
     int fr0, fr1, fr2;           // residues (molecule-relative) spanning the body frame
+    int tile_off, ntile;         // 32 x 32 intra tiles (ta <= tb) holding an unexcluded pair
 };
 
 // Delayed-acceptance counters of one replica slot (not swapped on exchange).
@@ -103,6 +104,7 @@ struct EngineArgs {
     const int *branch;
     const int *localres;
     const int *crankres;
+    const int2 *tiles;           // active intra tiles (ta, tb) of flexible molecules
     const float *table;          // Eij in kcal/mol, ntypes x ntypes (row stride 32)
     float4 *pos;
     float4 *rel;
@@ -132,7 +134,7 @@ struct EngineArgs {
     int max_n;                   // largest N
     int max_m;                   // largest M
     int max_mol;                 // largest molecule
-    int lmax[9];                 // largest per-simulation count of each static list
+    int lmax[10];                // largest per-simulation count of each static list
     // delayed acceptance with the learned surrogate (da != 0: k_mc<.., true> is launched)
     int da;
     const float *sur_P;          // FP32 master parameters
