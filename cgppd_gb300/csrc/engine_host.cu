@@ -382,19 +382,25 @@ int cgppd_engine::build()
                     angles.push_back(make_int4(an.i, an.j, an.k, 0));
                 dm.nang = (int)angles.size() - dm.ang_off;
                 dm.tor_off = (int)tors.size();
+                double vsum = 0.0;
                 for (const auto &t : G.torsions) {
                     tors.push_back(make_int4(t.i, t.j, t.k, t.l));
-                    float4 V{0, 0, 0, 0}, S{0, 0, 0, 0};
+                    // A_n = V_n cos(sigma_n), B_n = V_n sin(sigma_n) (torsion term by angle addition)
+                    float A[4] = {0, 0, 0, 0}, Bv[4] = {0, 0, 0, 0};
                     int a1 = hm.types[t.j], a2 = hm.types[t.k];
                     if (!torsV.empty() && a1 < tors_types && a2 < tors_types) {
                         const double *v = &torsV[4 * (a1 * tors_types + a2)];
                         const double *sg = &torsS[4 * (a1 * tors_types + a2)];
-                        V = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
-                        S = make_float4((float)sg[0], (float)sg[1], (float)sg[2], (float)sg[3]);
+                        for (int q = 0; q < 4; ++q) {
+                            A[q] = (float)(v[q] * std::cos(sg[q]));
+                            Bv[q] = (float)(v[q] * std::sin(sg[q]));
+                            vsum += v[q];
+                        }
                     }
-                    torsVv.push_back(V);
-                    torsSv.push_back(S);
+                    torsVv.push_back(make_float4(A[0], A[1], A[2], A[3]));
+                    torsSv.push_back(make_float4(Bv[0], Bv[1], Bv[2], Bv[3]));
                 }
+                dm.tors_const = (float)vsum;
                 dm.ntor = (int)tors.size() - dm.tor_off;
                 dm.ind_off = (int)indsub.size();
                 for (const auto &p : G.indirect_neighbours)

@@ -194,6 +194,27 @@ __device__ __forceinline__ double warp_sum_d(double v)
     return v;
 }
 
+__device__ __forceinline__ FF ff_from(double d)
+{
+    const float hi = (float)d;
+    return FF{hi, (float)(d - (double)hi)};
+}
+
+// Block-wide FF sum in a fixed order, returned (identically) in every thread.
+__device__ FF block_sum_ff_ff(FF v, FF *red)
+{
+    const int t = threadIdx.x, nw = blockDim.x >> 5;
+    v = ff_warp_sum(v);
+    __syncthreads();
+    if ((t & 31) == 0)
+        red[t >> 5] = v;
+    __syncthreads();
+    FF s{0.f, 0.f};
+    for (int w = 0; w < nw; ++w)
+        ff_add_ff(s, red[w]);
+    return s;
+}
+
 // Block-wide FF sum in a fixed order, returned as double in every thread.
 __device__ double block_sum_ff(FF v, FF *red)
 {
@@ -329,9 +350,13 @@ __device__ float bonded_item(const Lists &a, const DevMol &mol, const float4 *p,
         return -kGammaAngleRecip * logf(term);
     }
     // sum_n V_n (1 + cos(n phi - sigma_n))
+    // sum_n V_n (1 + cos(n phi - sigma_n)) = sum_n V_n + sum_n A_n cos(n phi) + B_n sin(n phi)
+    // with A_n = V_n cos(sigma_n), B_n = V_n sin(sigma_n) (precomputed); cos/sin(phi) from
+    // the dihedral's dot and cross products and cos/sin(n phi) by angle addition, so no
+    // atan2 or cos call sits on the step's path.  The molecule's sum of V_n is added once.
     const int ti = mol.tor_off + k - a.base[kLTor];
     const int4 tq = a.tors[ti];
-    const float4 V = a.torsV[ti], Sg = a.torsS[ti];
+    const float4 A = a.torsV[ti], B = a.torsS[ti];
     const float4 p1 = p[tq.x], p2 = p[tq.y], p3 = p[tq.z], p4 = p[tq.w];
     const float b1x = p2.x - p1.x, b1y = p2.y - p1.y, b1z = p2.z - p1.z;
     const float b2x = p3.x - p2.x, b2y = p3.y - p2.y, b2z = p3.z - p2.z;
@@ -339,9 +364,19 @@ __device__ float bonded_item(const Lists &a, const DevMol &mol, const float4 *p,
     const float c23x = b2y * b3z - b2z * b3y, c23y = b2z * b3x - b2x * b3z, c23z = b2x * b3y - b2y * b3x;
     const float c12x = b1y * b2z - b1z * b2y, c12y = b1z * b2x - b1x * b2z, c12z = b1x * b2y - b1y * b2x;
     const float mb2 = sqrtf(b2x * b2x + b2y * b2y + b2z * b2z);
-    const float phi = atan2f(mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), c12x * c23x + c12y * c23y + c12z * c23z);
-    return V.x * (1.f + cosf(phi - Sg.x)) + V.y * (1.f + cosf(2.f * phi - Sg.y)) +
-           V.z * (1.f + cosf(3.f * phi - Sg.z)) + V.w * (1.f + cosf(4.f * phi - Sg.w));
+    const float y = mb2 * (b1x * c23x + b1y * c23y + b1z * c23z), x = c12x * c23x + c12y * c23y + c12z * c23z;
+    const float h2 = x * x + y * y;
+    float c1 = 1.f, s1 = 0.f;  // atan2(0, 0) = 0
+    if (h2 > 0.f) {
+        const float inv = rsqrt_refined(h2);
+        c1 = x * inv;
+        s1 = y * inv;
+    }
+    const float c2 = c1 * c1 - s1 * s1, s2 = 2.f * s1 * c1;
+    const float c3 = c2 * c1 - s2 * s1, s3 = s2 * c1 + c2 * s1;
+    const float c4 = c3 * c1 - s3 * s1, s4 = s3 * c1 + c3 * s1;
+    const float e = ((A.x * c1 + B.x * s1) + (A.y * c2 + B.y * s2)) + ((A.z * c3 + B.z * s3) + (A.w * c4 + B.w * s4));
+    return (k == 0) ? e + mol.tors_const : e;
 }
 
 // Bonded terms of one molecule, one flat index over bonds, angles and torsions so that
@@ -732,7 +767,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     __shared__ MoveDesc mv;
     __shared__ FF s_red[kMaxWarps];
     __shared__ float s_fred[3 * kMaxWarps];
-    __shared__ double s_old_row, s_pot, s_intrap, s_intra_new, s_new_row;
+    // running total, old/new row of the moved molecule and its internal energy, all as
+    // float-float pairs so that the step's decision path has no FP64 arithmetic
+    __shared__ FF s_pot, s_old_row, s_intrap, s_intra_new, s_new_row;
     __shared__ int s_accept;
     __shared__ DevSim S;           // this replica's simulation (read by thread 0 mostly)
     __shared__ ReplicaStats st;    // counters, updated by thread 0
@@ -772,8 +809,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     float4 *s_disp = reinterpret_cast<float4 *>(smem + Ly.idisp);
     float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
     float2 *s_ej = reinterpret_cast<float2 *>(smem + Ly.ej);
-    double *s_rowp = reinterpret_cast<double *>(smem + Ly.rowp);
-    double *s_row = reinterpret_cast<double *>(smem + Ly.row);
+    FF *s_rowp = reinterpret_cast<FF *>(smem + Ly.rowp);
+    FF *s_row = reinterpret_cast<FF *>(smem + Ly.row);
 
     const long long st0 = S.state_off + (long long)r * N;
     float4 *gP = a.pos + st0;
@@ -897,7 +934,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     }
     const Lists &Ls = s_lists;
     if (t == 0)
-        s_pot = __ldcg(&a.potential[g]);
+        s_pot = ff_from(__ldcg(&a.potential[g]));
     __syncthreads();
     DaView &dv = s_dv;
     if (DA) {
@@ -921,7 +958,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             for (int k = 0; k < 12; ++k)
                 w[k] = s_w[k];
             decide_move<RES>(Ls, S, s_mols, CEN, P, tstep, rstep, rsc, w, mv);
-            s_old_row = RES ? ROWSUM[mv.m] : 0.0;
+            if (RES)
+                s_old_row = ff_from(ROWSUM[mv.m]);
         }
         __syncthreads();
         const int n = mv.n, start = mv.start, type = mv.type, m = mv.m;
@@ -971,7 +1009,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     v += __ldcg(&EM[(long long)m * M + b]);
             v = warp_sum_d(v);
             if (lane == 0)
-                s_old_row = v + __ldcg(&INTRA[m]);
+                s_old_row = ff_from(v + __ldcg(&INTRA[m]));
         }
 
         // ---- proposal of the moved molecule
@@ -1187,7 +1225,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         // In a cluster every CTA pushes its partials into every CTA's receive slots
         // (step parity, source rank) before the barrier, so nothing is read remotely after it.
         const int M1 = a.max_m + 1;
-        double *rcv = reinterpret_cast<double *>(smem + Ly.rcv) + (step & 1) * C * M1;
+        FF *rcv = reinterpret_cast<FF *>(smem + Ly.rcv) + (step & 1) * C * M1;
         for (int b = warp; b < M; b += NW) {
             FF acc{0.f, 0.f};
             if (b != m) {
@@ -1201,7 +1239,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 acc = ff_warp_sum(acc);
             }
             // lane 0's value for every receiver (lanes may differ in the low word)
-            const double v = __shfl_sync(0xffffffffu, (b != m) ? ff_value(acc) : 0.0, 0);
+            const FF v{__shfl_sync(0xffffffffu, (b != m) ? acc.hi : 0.f, 0),
+                       __shfl_sync(0xffffffffu, (b != m) ? acc.lo : 0.f, 0)};
             if (C > 1) {
                 if (lane < C)
                     cg::this_cluster().map_shared_rank(rcv, lane)[rank * M1 + b] = v;
@@ -1210,7 +1249,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
         }
         if (flexmol) {
-            const double v = block_sum_ff(iacc, s_red);
+            const FF v = block_sum_ff_ff(iacc, s_red);
             if (C > 1) {
                 if (t < C)
                     cg::this_cluster().map_shared_rank(rcv, t)[rank * M1 + a.max_m] = v;
@@ -1224,40 +1263,42 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             __syncthreads();
 
         // ---- sum the cluster's partials (fixed rank order, local reads) and take the
-        // Metropolis decision, all in warp 0 (no CTA barrier before the decision)
-        const double *rowv = (C > 1) ? s_row : s_rowp;
+        // Metropolis decision, all in warp 0 (no CTA barrier before the decision) and in
+        // float-float arithmetic (FP32 pipe; the FP64 unit is slow on this part)
+        const FF *rowv = (C > 1) ? s_row : s_rowp;
         if (warp == 0) {
-            double v = 0.0;
+            FF v{0.f, 0.f};
             for (int b = lane; b < M; b += 32) {
-                double rb;
+                FF rb{0.f, 0.f};
                 if (C > 1) {
-                    rb = 0.0;
                     for (int k = 0; k < C; ++k)
-                        rb += rcv[k * M1 + b];
+                        ff_add_ff(rb, rcv[k * M1 + b]);
                     s_row[b] = rb;
                 } else {
                     rb = s_rowp[b];
                 }
                 if (b != m)
-                    v += rb;
+                    ff_add_ff(v, rb);
             }
-            v = warp_sum_d(v);
+            v = ff_warp_sum(v);
             if (lane == 0) {
-                double intra_new = 0.0;
+                FF intra_new{0.f, 0.f};
                 if (flexmol) {
                     if (C > 1)
                         for (int k = 0; k < C; ++k)
-                            intra_new += rcv[k * M1 + a.max_m];
+                            ff_add_ff(intra_new, rcv[k * M1 + a.max_m]);
                     else
                         intra_new = s_intrap;
                 }
                 s_intra_new = intra_new;
-                const double new_row = v + intra_new;
+                FF new_row = v;
+                ff_add_ff(new_row, intra_new);
                 s_new_row = new_row;
-                const double dE = new_row - s_old_row;  // = newPotential - oldPotential
-                float delta = (float)dE;
+                FF dEf = new_row;  // newPotential - oldPotential = new row - old row
+                ff_add_ff(dEf, FF{-s_old_row.hi, -s_old_row.lo});
+                float delta = dEf.hi + dEf.lo;
                 if (DA && screened)  // stage 2: exact change less the surrogate's
-                    delta = (float)(dE - s_ds);
+                    delta = (float)(ff_value(dEf) - s_ds);
                 int acc = 0;
                 if (delta < 0.0f) {
                     acc = 1;
@@ -1268,11 +1309,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     const unsigned long long thr = (unsigned long long)ceilf(boltz * 4294967296.0f);
                     acc = ((unsigned long long)mv.w_metro < thr) ? 2 : 0;
                 }
-                if (!isfinite(dE))
+                if (!isfinite(dEf.hi))
                     acc = 0;
-                const double newPotential = s_pot - s_old_row + new_row;
                 if (DA && screened) {
-                    const double e = dE - s_ds;
+                    const double dE = ff_value(dEf), e = dE - s_ds;
                     s_da.stage2_eval++;
                     if (acc)
                         s_da.stage2_accept++;
@@ -1284,8 +1324,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     }
                 }
                 s_accept = acc;
-                if (acc)
-                    s_pot = newPotential;
+                if (acc) {
+                    FF pot = s_pot;
+                    ff_add_ff(pot, dEf);
+                    s_pot = pot;
+                }
                 if (acc == 1)
                     st.accept++;
                 else if (acc == 2)
@@ -1312,16 +1355,16 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
             for (int b = t; b < M; b += T) {
                 if (b != m) {
-                    const double nv = rowv[b];
+                    const double nv = ff_value(rowv[b]);
                     if (RES)
                         ROWSUM[b] += nv - EM[(long long)m * M + b];
                     EM[(long long)m * M + b] = nv;
                     EM[(long long)b * M + m] = nv;
                 } else {
                     if (RES)
-                        ROWSUM[m] = s_new_row;
+                        ROWSUM[m] = ff_value(s_new_row);
                     if (flexmol)
-                        INTRA[m] = s_intra_new;
+                        INTRA[m] = ff_value(s_intra_new);
                 }
             }
             if (t == 0)
@@ -1355,7 +1398,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     }
                     e = warp_sum_d(e);
                 } else if (S.nc_mode == 2) {
-                    e = s_pot;
+                    e = ff_value(s_pot);
                 }
                 if (lane == 0) {
                     st.samplesSinceLastExchange++;
@@ -1391,7 +1434,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 gE[k] = EM[k];
         }
         if (t == 0) {
-            a.potential[g] = s_pot;
+            a.potential[g] = ff_value(s_pot);
             a.stats[g] = st;
             if (DA)
                 a.dastats[g] = s_da;

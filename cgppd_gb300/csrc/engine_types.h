@@ -64,6 +64,7 @@ struct DevMol {
     int nintra;                  // intra pairs that are not excluded (flexible molecules)
     int fr0, fr1, fr2;           // residues (molecule-relative) spanning the body frame
     int tile_off, ntile;         // 32 x 32 intra tiles (ta <= tb) holding an unexcluded pair
+    float tors_const;            // sum of V_n over the molecule's torsions (kcal/mol)
 };
 
 // Delayed-acceptance counters of one replica slot (not swapped on exchange).
@@ -96,8 +97,8 @@ struct EngineArgs {
     const int2 *bonds;
     const int4 *angles;          // (i, j, k, 0)
     const int4 *tors;            // (i, j, k, l)
-    const float4 *torsV;         // amplitudes V1..V4 of each torsion
-    const float4 *torsS;         // phases (rad) of each torsion
+    const float4 *torsV;         // V_n cos(sigma_n), n = 1..4, of each torsion
+    const float4 *torsS;         // V_n sin(sigma_n)
     const int2 *indsub;
     const int4 *flexres;         // (ri, degree, first option, 0)
     const int4 *flexopt;         // (neighbour, branch offset, branch count, 0)
