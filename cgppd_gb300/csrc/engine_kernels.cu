@@ -827,9 +827,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     const float4 *ST = RES ? reinterpret_cast<const float4 *>(smem + Ly.ST) : gST;
     const int4 *EX = (RES && a.any_flexible) ? reinterpret_cast<const int4 *>(smem + Ly.EX) : gEX;
     float4 *CEN = RES ? reinterpret_cast<float4 *>(smem + Ly.CEN) : gCEN;
-    double *EM = RES ? reinterpret_cast<double *>(smem + Ly.EM) : gE;
-    double *INTRA = RES ? reinterpret_cast<double *>(smem + Ly.INTRA) : gINTRA;
-    double *ROWSUM = RES ? reinterpret_cast<double *>(smem + Ly.ROWSUM) : nullptr;
+    // resident copies of the pair matrix, internal energies and row sums are float-float
+    // (converted from / to the global doubles at launch start and end)
+    FF *EMf = reinterpret_cast<FF *>(smem + Ly.EM);
+    FF *INTRAf = reinterpret_cast<FF *>(smem + Ly.INTRA);
+    FF *ROWSUMf = reinterpret_cast<FF *>(smem + Ly.ROWSUM);
 
     for (int k = t; k < kTableStride * kTableStride; k += T)
         s_table[k] = a.table[k];
@@ -850,18 +852,18 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         }
         for (int k = t; k < M; k += T) {
             sC[k] = __ldcg(&gCEN[k]);
-            INTRA[k] = __ldcg(&gINTRA[k]);
+            INTRAf[k] = ff_from(__ldcg(&gINTRA[k]));
         }
         for (int k = t; k < M * M; k += T)
-            EM[k] = __ldcg(&gE[k]);
+            EMf[k] = ff_from(__ldcg(&gE[k]));
         __syncthreads();
         // row sums: S[m] = intra[m] + sum_b E[m][b]
         for (int k = t; k < M; k += T) {
-            double v = INTRA[k];
+            FF v = INTRAf[k];
             for (int b = 0; b < M; ++b)
                 if (b != k)
-                    v += EM[(long long)k * M + b];
-            ROWSUM[k] = v;
+                    ff_add_ff(v, EMf[(long long)k * M + b]);
+            ROWSUMf[k] = v;
         }
     }
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
@@ -959,7 +961,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 w[k] = s_w[k];
             decide_move<RES>(Ls, S, s_mols, CEN, P, tstep, rstep, rsc, w, mv);
             if (RES)
-                s_old_row = ff_from(ROWSUM[mv.m]);
+                s_old_row = ROWSUMf[mv.m];
         }
         __syncthreads();
         const int n = mv.n, start = mv.start, type = mv.type, m = mv.m;
@@ -1006,10 +1008,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             double v = 0.0;
             for (int b = lane; b < M; b += 32)
                 if (b != m)
-                    v += __ldcg(&EM[(long long)m * M + b]);
+                    v += __ldcg(&gE[(long long)m * M + b]);
             v = warp_sum_d(v);
             if (lane == 0)
-                s_old_row = ff_from(v + __ldcg(&INTRA[m]));
+                s_old_row = ff_from(v + __ldcg(&gINTRA[m]));
         }
 
         // ---- proposal of the moved molecule
@@ -1103,10 +1105,19 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int nother = N - n;
         const int o0 = rank * slice, o1 = min(nother, o0 + slice);
         const int cnt = max(0, o1 - o0);
+        // threads per j (each takes every tpj-th i): the power of two that minimises the
+        // busiest thread's pair count, passes x ceil(n / tpj) (the smaller on ties)
         int tpj = 1;
-        if (cnt > 0)
-            while (tpj < 32 && cnt * tpj * 2 <= T)
-                tpj <<= 1;
+        if (cnt > 0) {
+            int best = ((cnt + T - 1) / T) * n;
+            for (int c = 2; c <= 32 && c <= n; c <<= 1) {
+                const int w = ((cnt * c + T - 1) / T) * ((n + c - 1) / c);
+                if (w < best) {
+                    best = w;
+                    tpj = c;
+                }
+            }
+        }
         const int sub = t & (tpj - 1), jl = t / tpj, jstride = T / tpj;
         // residue record of this thread's next j, loaded one iteration ahead
         float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
@@ -1355,16 +1366,28 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
             for (int b = t; b < M; b += T) {
                 if (b != m) {
-                    const double nv = ff_value(rowv[b]);
-                    if (RES)
-                        ROWSUM[b] += nv - EM[(long long)m * M + b];
-                    EM[(long long)m * M + b] = nv;
-                    EM[(long long)b * M + m] = nv;
+                    if (RES) {
+                        const FF nv = rowv[b], ov = EMf[(long long)m * M + b];
+                        FF rs = ROWSUMf[b];
+                        ff_add_ff(rs, nv);
+                        ff_add_ff(rs, FF{-ov.hi, -ov.lo});
+                        ROWSUMf[b] = rs;
+                        EMf[(long long)m * M + b] = nv;
+                        EMf[(long long)b * M + m] = nv;
+                    } else {
+                        const double nv = ff_value(rowv[b]);
+                        gE[(long long)m * M + b] = nv;
+                        gE[(long long)b * M + m] = nv;
+                    }
                 } else {
                     if (RES)
-                        ROWSUM[m] = ff_value(s_new_row);
-                    if (flexmol)
-                        INTRA[m] = ff_value(s_intra_new);
+                        ROWSUMf[m] = s_new_row;
+                    if (flexmol) {
+                        if (RES)
+                            INTRAf[m] = s_intra_new;
+                        else
+                            gINTRA[m] = ff_value(s_intra_new);
+                    }
                 }
             }
             if (t == 0)
@@ -1394,7 +1417,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     for (int k = lane; k < nc * nc; k += 32) {
                         const int aa = k / nc, bb = k % nc;
                         if (aa < bb)
-                            e += ld_state<RES>(&EM[(long long)aa * M + bb]);
+                            e += RES ? ff_value(EMf[(long long)aa * M + bb]) : __ldcg(&gE[(long long)aa * M + bb]);
                     }
                     e = warp_sum_d(e);
                 } else if (S.nc_mode == 2) {
@@ -1428,10 +1451,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
             for (int k = t; k < M; k += T) {
                 gCEN[k] = CEN[k];
-                gINTRA[k] = INTRA[k];
+                gINTRA[k] = ff_value(INTRAf[k]);
             }
             for (int k = t; k < M * M; k += T)
-                gE[k] = EM[k];
+                gE[k] = ff_value(EMf[k]);
         }
         if (t == 0) {
             a.potential[g] = ff_value(s_pot);
