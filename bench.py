@@ -313,26 +313,33 @@ def gpu_arm(args):
     # and potentials, every step
     e2e = None
     if not args.no_e2e:
-        N, M, Rs = e.sim_info(0)
-        hp = torch.empty((Rs * N * 4,), dtype=torch.float32).pin_memory()
-        hr = torch.empty((Rs * N * 4,), dtype=torch.float32).pin_memory()
-        hc = torch.empty((Rs * M * 4,), dtype=torch.float32).pin_memory()
-        hpot = torch.empty((Rs,), dtype=torch.float64).pin_memory()
-        e.download(0, hp.data_ptr(), hr.data_ptr(), hc.data_ptr(), hpot.data_ptr(), stream=sh)
+        sims = []
+        for si in range(len(wl.sims)):
+            N, M, Rs = e.sim_info(si)
+            bufs = (torch.empty((Rs * N * 4,), dtype=torch.float32).pin_memory(),
+                    torch.empty((Rs * N * 4,), dtype=torch.float32).pin_memory(),
+                    torch.empty((Rs * M * 4,), dtype=torch.float32).pin_memory(),
+                    torch.empty((Rs,), dtype=torch.float64).pin_memory())
+            sims.append((si, N, M, Rs, bufs))
+            e.download(si, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(), bufs[3].data_ptr(), stream=sh)
         stream.synchronize()
         n_e2e = max(2, args.steps // 2)
         barrier()
         t0 = time.perf_counter()
         s0 = e.counters()[0]
         for _ in range(n_e2e):
-            e.upload(0, hp.data_ptr(), hr.data_ptr(), hc.data_ptr(), recompute=True, stream=sh)
+            # the last upload re-evaluates every replica of every simulation (one launch)
+            for si, N, M, Rs, b in sims:
+                e.upload(si, b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(), recompute=(si == len(sims) - 1),
+                         stream=sh)
             e.run(1, K, True, stream=sh)
-            e.download(0, hp.data_ptr(), hr.data_ptr(), hc.data_ptr(), hpot.data_ptr(), stream=sh)
+            for si, N, M, Rs, b in sims:
+                e.download(si, b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(), b[3].data_ptr(), stream=sh)
             stream.synchronize()
         t1 = time.perf_counter()
         done = e.counters()[0] - s0
-        h2d = (2 * Rs * N + Rs * M) * 16
-        d2h = h2d + Rs * 8
+        h2d = sum((2 * Rs * N + Rs * M) * 16 for _, N, M, Rs, _ in sims)
+        d2h = h2d + sum(Rs * 8 for _, _, _, Rs, _ in sims)
         tt = torch.tensor([t1 - t0], dtype=torch.float64, device="cuda")
         if dist:
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)

@@ -1105,19 +1105,12 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int nother = N - n;
         const int o0 = rank * slice, o1 = min(nother, o0 + slice);
         const int cnt = max(0, o1 - o0);
-        // threads per j (each takes every tpj-th i): the power of two that minimises the
-        // busiest thread's pair count, passes x ceil(n / tpj) (the smaller on ties)
+        // threads per j (each takes every tpj-th i): split the i loop only while the slice
+        // leaves threads idle (long per-thread loops keep the 4-way partial sums busy)
         int tpj = 1;
-        if (cnt > 0) {
-            int best = ((cnt + T - 1) / T) * n;
-            for (int c = 2; c <= 32 && c <= n; c <<= 1) {
-                const int w = ((cnt * c + T - 1) / T) * ((n + c - 1) / c);
-                if (w < best) {
-                    best = w;
-                    tpj = c;
-                }
-            }
-        }
+        if (cnt > 0)
+            while (tpj < 32 && cnt * tpj * 2 <= T)
+                tpj <<= 1;
         const int sub = t & (tpj - 1), jl = t / tpj, jstride = T / tpj;
         // residue record of this thread's next j, loaded one iteration ahead
         float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
