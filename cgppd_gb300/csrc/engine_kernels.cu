@@ -315,92 +315,6 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
     return lj + dh_term(qa.x * qb.x, r, inv_r);
 }
 
-// ---- two pair terms at once on the packed FP32 unit (add/sub/mul/fma .f32x2): the
-// terms (a0, b) and (a1, b), element-wise the same IEEE operations as pair_kcal with no
-// FMA contraction; MUFU (rsqrt, ex2), rint, the table lookups and the repulsive-branch
-// select stay per element.  Halves the FP32 instruction count of the pair loop.
-typedef unsigned long long f32x2;
-
-__device__ __forceinline__ f32x2 f2p(float lo, float hi)
-{
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2u(f32x2 v, float &lo, float &hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f32x2 f2add(f32x2 a, f32x2 b)
-{
-    f32x2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2sub(f32x2 a, f32x2 b)
-{
-    f32x2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b)
-{
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c)
-{
-    f32x2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
-__device__ __forceinline__ f32x2 min_image2(f32x2 d, f32x2 nL, f32x2 invL)
-{
-    float t0, t1;
-    f2u(f2mul(d, invL), t0, t1);
-    return f2fma(nL, f2p(rintf(t0), rintf(t1)), d);
-}
-
-__device__ __forceinline__ f32x2 pair_kcal2(float4 a0, float2 qa0, float4 a1, float2 qa1, float4 b, float2 qb,
-                                            const float *table, float L, float invL)
-{
-    const f32x2 nL = f2p(-L, -L), iL = f2p(invL, invL);
-    const f32x2 dx = min_image2(f2sub(f2p(a0.x, a1.x), f2p(b.x, b.x)), nL, iL);
-    const f32x2 dy = min_image2(f2sub(f2p(a0.y, a1.y), f2p(b.y, b.y)), nL, iL);
-    const f32x2 dz = min_image2(f2sub(f2p(a0.z, a1.z), f2p(b.z, b.z)), nL, iL);
-    const f32x2 r2 = f2fma(dx, dx, f2fma(dy, dy, f2mul(dz, dz)));
-    float r20, r21;
-    f2u(r2, r20, r21);
-    const f32x2 y = f2p(rsqrtf(r20), rsqrtf(r21));
-    // rsqrt_refined: y * (1.5 - (0.5 r2 y) y)
-    const f32x2 h = f2mul(f2mul(f2p(0.5f, 0.5f), r2), y);
-    const f32x2 inv_r = f2mul(y, f2fma(f2sub(f2p(0.f, 0.f), h), y, f2p(1.5f, 1.5f)));
-    const f32x2 r = f2mul(r2, inv_r);
-    const int tb = __float_as_int(qb.y);
-    const float e0 = table[__float_as_int(qa0.y) * kTableStride + tb];
-    const float e1 = table[__float_as_int(qa1.y) * kTableStride + tb];
-    const f32x2 eij = f2p(e0, e1);
-    // lj_term: s6 = (sigma^2 / r^2)^3, u = -4 eij s6 (s6 - 1), repulsive branch 2 eij - u
-    const f32x2 sig = f2add(f2p(a0.w, a1.w), f2p(b.w, b.w));
-    const f32x2 s2 = f2mul(f2mul(sig, sig), f2mul(inv_r, inv_r));
-    const f32x2 s6 = f2mul(f2mul(s2, s2), s2);
-    const f32x2 u = f2mul(f2mul(f2mul(f2p(-4.0f, -4.0f), eij), s6), f2sub(s6, f2p(1.0f, 1.0f)));
-    const f32x2 ur = f2fma(f2p(2.0f, 2.0f), eij, f2sub(f2p(0.f, 0.f), u));
-    float u0, u1, ur0, ur1, s60, s61;
-    f2u(u, u0, u1);
-    f2u(ur, ur0, ur1);
-    f2u(s6, s60, s61);
-    const f32x2 lj = f2p((e0 > 0.0f && s60 > 0.5f) ? ur0 : u0, (e1 > 0.0f && s61 > 0.5f) ? ur1 : u1);
-    // dh_term: qq exp2(-r log2(e) / xi) / r
-    const f32x2 qq = f2mul(f2p(qa0.x, qa1.x), f2p(qb.x, qb.x));
-    float x0, x1;
-    f2u(f2mul(r, f2p(-kLog2e / kXi, -kLog2e / kXi)), x0, x1);
-    const f32x2 dh = f2mul(f2mul(qq, f2p(exp2f(x0), exp2f(x1))), inv_r);
-    return f2add(lj, dh);
-}
-
 __device__ __forceinline__ bool intra_excluded(int4 ei, int4 ej)
 {
     // same rigid domain, backbone neighbours (|resSeq| < 4 on one chain), or bonded
@@ -1220,26 +1134,19 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 const float2 qj = make_float2(sj.y, sj.z);
                 // four independent partial sums (instruction-level parallelism), folded
                 // into the float-float accumulator every 32 terms
-                // four pair terms per iteration in two packed pairs, four partial sums
-                f32x2 pa = f2p(0.f, 0.f), pb = pa;
+                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
                 int i = sub, cntp = 0;
                 for (; i + 3 * tpj < n; i += 4 * tpj) {
-                    pa = f2add(pa, pair_kcal2(s_ipos[i], s_iq[i], s_ipos[i + tpj], s_iq[i + tpj], rj, qj, s_table,
-                                              L, invL));
-                    pb = f2add(pb, pair_kcal2(s_ipos[i + 2 * tpj], s_iq[i + 2 * tpj], s_ipos[i + 3 * tpj],
-                                              s_iq[i + 3 * tpj], rj, qj, s_table, L, invL));
+                    p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                    p1 += pair_kcal(s_ipos[i + tpj], s_iq[i + tpj], rj, qj, s_table, L, invL);
+                    p2 += pair_kcal(s_ipos[i + 2 * tpj], s_iq[i + 2 * tpj], rj, qj, s_table, L, invL);
+                    p3 += pair_kcal(s_ipos[i + 3 * tpj], s_iq[i + 3 * tpj], rj, qj, s_table, L, invL);
                     if (++cntp == 8) {
-                        float p0, p1, p2, p3;
-                        f2u(pa, p0, p1);
-                        f2u(pb, p2, p3);
                         ff_add(acc, (p0 + p1) + (p2 + p3));
-                        pa = pb = f2p(0.f, 0.f);
+                        p0 = p1 = p2 = p3 = 0.f;
                         cntp = 0;
                     }
                 }
-                float p0, p1, p2, p3;
-                f2u(pa, p0, p1);
-                f2u(pb, p2, p3);
                 for (; i < n; i += tpj)
                     p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
                 ff_add(acc, (p0 + p1) + (p2 + p3));
