@@ -113,7 +113,7 @@ void frame_residues(const HostMolecule &hm, int &f0, int &f1, int &f2)
 }  // namespace
 
 struct cgppd_engine {
-    std::vector<float> table;  // Eij kcal, 32x32
+    std::vector<float> table;  // -4 Eij kcal/mol, 32x32
     std::vector<double> torsV, torsS;
     int tors_types = 0;
     int ntypes = 0;
@@ -674,7 +674,7 @@ cgppd_engine *cgppd_engine_create(const float *lj_raw, int ntypes, const double 
     // (src/Potential.cpp:14), then in kcal/mol.
     for (int i = 0; i < ntypes; ++i)
         for (int j = 0; j < ntypes; ++j)
-            e->table[i * 32 + j] = (kLambda * (lj_raw[i * ntypes + j] - kE0)) * kRTtoKcal;
+            e->table[i * 32 + j] = -4.0f * ((kLambda * (lj_raw[i * ntypes + j] - kE0)) * kRTtoKcal);
     if (torsion_V && torsion_phase && torsion_types > 0) {
         e->tors_types = torsion_types;
         e->torsV.assign(torsion_V, torsion_V + 4 * torsion_types * torsion_types);

@@ -299,8 +299,19 @@ __device__ __forceinline__ float3 normalized(float x, float y, float z)
     return make_float3(x, y, z);
 }
 
+// 2^x on the SFU (PTX ex2.approx.ftz.f32, max relative error 2^-22); the Debye-Hueckel
+// argument -r log2(e) / xi stays far from the denormal range for r > 0.
+__device__ __forceinline__ float ex2_sfu(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with
-// (q*sqrt(DHF), type) in qa/qb.
+// (q*sqrt(DHF), type) in qa/qb.  `table` holds -4 Eij (kcal/mol): the LJ term is
+// u = (-4 Eij) s6 (s6 - 1), and 2 Eij - u on the repulsive branch (Eij > 0, s6 > 1/2),
+// the same values as lj_term with one multiplication less (power-of-two scaling).
 __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float *table, float L,
                                            float invL)
 {
@@ -310,9 +321,14 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float inv_r = rsqrt_refined(r2);
     const float r = r2 * inv_r;
-    const float eij = table[__float_as_int(qa.y) * kTableStride + __float_as_int(qb.y)];
-    const float lj = lj_term(eij, a.w + b.w, inv_r * inv_r);
-    return lj + dh_term(qa.x * qb.x, r, inv_r);
+    const float m4e = table[__float_as_int(qa.y) * kTableStride + __float_as_int(qb.y)];
+    const float so = (a.w + b.w) * inv_r;  // sigma_ij / r
+    const float s2 = so * so;
+    const float s6 = s2 * s2 * s2;
+    float u = m4e * s6 * (s6 - 1.0f);
+    if (m4e < 0.0f && s6 > 0.5f)
+        u = fmaf(-0.5f, m4e, -u);
+    return u + qa.x * qb.x * ex2_sfu(r * (-kLog2e / kXi)) * inv_r;
 }
 
 __device__ __forceinline__ bool intra_excluded(int4 ei, int4 ej)

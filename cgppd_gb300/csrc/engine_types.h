@@ -106,7 +106,7 @@ struct EngineArgs {
     const int *localres;
     const int *crankres;
     const int2 *tiles;           // active intra tiles (ta, tb) of flexible molecules
-    const float *table;          // Eij in kcal/mol, ntypes x ntypes (row stride 32)
+    const float *table;          // -4 Eij in kcal/mol, ntypes x ntypes (row stride 32)
     float4 *pos;
     float4 *rel;
     float4 *center;
