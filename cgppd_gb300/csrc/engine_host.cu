@@ -1076,6 +1076,143 @@ int cgppd_engine_download(cgppd_engine *e, int sim, float *pos4, float *rel4, fl
     return rc ? -1 : 0;
 }
 
+}  // extern "C"
+
+// ---- checkpoint / restore: every mutable device buffer of the engine in one file.
+// Layout: magic "CGPPDCK1", u64 fingerprint length + fingerprint (the system's shape),
+// then for each buffer u64 byte count + bytes, in a fixed order.
+static std::vector<long long> engine_fingerprint(const cgppd_engine *e)
+{
+    std::vector<long long> f{(long long)e->sims.size(), e->total_replicas, e->max_n, e->max_m};
+    for (const auto &s : e->h_sims) {
+        f.push_back(s.N);
+        f.push_back(s.M);
+        f.push_back(s.R);
+    }
+    for (const auto &m : e->h_mols) {
+        f.push_back(m.start);
+        f.push_back(m.count);
+        f.push_back(m.flags);
+    }
+    return f;
+}
+
+template <typename F>
+static int for_each_state_buffer(cgppd_engine *e, F &&f)
+{
+    int rc = 0;
+    rc |= f(e->d_pos.ptr, e->d_pos.n * sizeof(float4));
+    rc |= f(e->d_rel.ptr, e->d_rel.n * sizeof(float4));
+    rc |= f(e->d_center.ptr, e->d_center.n * sizeof(float4));
+    rc |= f(e->d_emat.ptr, e->d_emat.n * sizeof(double));
+    rc |= f(e->d_intra.ptr, e->d_intra.n * sizeof(double));
+    rc |= f(e->d_potential.ptr, e->d_potential.n * sizeof(double));
+    rc |= f(e->d_temperature.ptr, e->d_temperature.n * sizeof(float));
+    rc |= f(e->d_tstep.ptr, e->d_tstep.n * sizeof(float));
+    rc |= f(e->d_rstep.ptr, e->d_rstep.n * sizeof(double));
+    rc |= f(e->d_stepc.ptr, e->d_stepc.n * sizeof(unsigned long long));
+    rc |= f(e->d_pairc.ptr, e->d_pairc.n * sizeof(unsigned long long));
+    rc |= f(e->d_stats.ptr, e->d_stats.n * sizeof(ReplicaStats));
+    rc |= f(e->d_tindex.ptr, e->d_tindex.n * sizeof(int));
+    rc |= f(e->d_label.ptr, e->d_label.n * sizeof(int));
+    rc |= f(e->d_slot_of_t.ptr, e->d_slot_of_t.n * sizeof(int));
+    rc |= f(e->d_sim_state.ptr, e->d_sim_state.n * sizeof(int));
+    rc |= f(e->d_errflags.ptr, e->d_errflags.n * sizeof(unsigned));
+    rc |= f(e->d_dastats.ptr, e->d_dastats.n * sizeof(DAStats));
+    rc |= f(e->d_sim_da.ptr, e->d_sim_da.n * sizeof(int));
+    rc |= f(e->d_report.ptr, (size_t)e->report_capacity * e->total_replicas * sizeof(float4));
+    rc |= f(e->d_exch_report.ptr, (size_t)e->report_capacity * e->sims.size() * sizeof(int2));
+    return rc;
+}
+
+extern "C" int cgppd_engine_checkpoint(cgppd_engine *e, const char *path)
+{
+    if (!e || !e->finalized || !path)
+        return cgppd_fail("cgppd_engine_checkpoint: engine not finalized or no path");
+    if (cgppd_check(cudaStreamSynchronize(e->own_stream), "checkpoint") != 0 ||
+        cgppd_check(cudaDeviceSynchronize(), "checkpoint") != 0)
+        return -1;
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp)
+        return cgppd_fail("cgppd_engine_checkpoint: cannot open the file for writing");
+    const std::vector<long long> fpr = engine_fingerprint(e);
+    const uint64_t nf = fpr.size(), cap = (uint64_t)e->report_capacity;
+    bool ok = std::fwrite("CGPPDCK1", 1, 8, fp) == 8 && std::fwrite(&nf, 8, 1, fp) == 1 &&
+              std::fwrite(fpr.data(), sizeof(long long), nf, fp) == nf && std::fwrite(&cap, 8, 1, fp) == 1;
+    std::vector<unsigned char> host;
+    const int rc = for_each_state_buffer(e, [&](void *dptr, size_t bytes) -> int {
+        const uint64_t nb = bytes;
+        if (!ok || std::fwrite(&nb, 8, 1, fp) != 1) {
+            ok = false;
+            return -1;
+        }
+        if (bytes == 0)
+            return 0;
+        host.resize(bytes);
+        if (cgppd_check(cudaMemcpy(host.data(), dptr, bytes, cudaMemcpyDeviceToHost), "checkpoint copy") != 0)
+            return -1;
+        if (std::fwrite(host.data(), 1, bytes, fp) != bytes) {
+            ok = false;
+            return -1;
+        }
+        return 0;
+    });
+    ok = (std::fclose(fp) == 0) && ok;
+    if (rc != 0 || !ok)
+        return cgppd_fail("cgppd_engine_checkpoint: write failed");
+    return 0;
+}
+
+extern "C" int cgppd_engine_restore(cgppd_engine *e, const char *path)
+{
+    if (!e || !e->finalized || !path)
+        return cgppd_fail("cgppd_engine_restore: engine not finalized or no path");
+    if (cgppd_check(cudaDeviceSynchronize(), "restore") != 0)
+        return -1;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp)
+        return cgppd_fail("cgppd_engine_restore: cannot open the file");
+    char magic[8];
+    uint64_t nf = 0, cap = 0;
+    bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, "CGPPDCK1", 8) == 0 &&
+              std::fread(&nf, 8, 1, fp) == 1 && nf < (1u << 26);
+    std::vector<long long> fpr(ok ? nf : 0);
+    ok = ok && std::fread(fpr.data(), sizeof(long long), nf, fp) == nf && std::fread(&cap, 8, 1, fp) == 1;
+    if (!ok || fpr != engine_fingerprint(e)) {
+        std::fclose(fp);
+        return cgppd_fail("cgppd_engine_restore: not a checkpoint of an engine with this system");
+    }
+    if (cap > (uint64_t)e->report_capacity && ensure_reports(e, (int)cap) != 0) {
+        std::fclose(fp);
+        return -1;
+    }
+    std::vector<unsigned char> host;
+    const int saved_cap = e->report_capacity;
+    e->report_capacity = (int)cap;  // the report buffers are read for the saved rows only
+    const int rc = for_each_state_buffer(e, [&](void *dptr, size_t bytes) -> int {
+        uint64_t nb = 0;
+        if (!ok || std::fread(&nb, 8, 1, fp) != 1 || nb != bytes) {
+            ok = false;
+            return -1;
+        }
+        if (bytes == 0)
+            return 0;
+        host.resize(bytes);
+        if (std::fread(host.data(), 1, bytes, fp) != bytes) {
+            ok = false;
+            return -1;
+        }
+        return cgppd_check(cudaMemcpy(dptr, host.data(), bytes, cudaMemcpyHostToDevice), "restore copy");
+    });
+    e->report_capacity = saved_cap;
+    std::fclose(fp);
+    if (rc != 0 || !ok)
+        return cgppd_fail("cgppd_engine_restore: truncated or mismatched checkpoint");
+    return 0;
+}
+
+extern "C" {
+
 int cgppd_engine_get_matrix(cgppd_engine *e, int sim, int replica, double *E, double *intra)
 {
     if (sim < 0 || sim >= (int)e->h_sims.size() || replica < 0 || replica >= e->h_sims[sim].R)

@@ -45,6 +45,8 @@ _DECL = {
     "cgppd_engine_last_launches": (c_int, [c_void_p]),
     "cgppd_engine_launch_shape": (c_int, [c_void_p, P(c_int), P(c_int)]),
     "cgppd_engine_set_resident": (c_int, [c_void_p, c_int]),
+    "cgppd_engine_checkpoint": (c_int, [c_void_p, ctypes.c_char_p]),
+    "cgppd_engine_restore": (c_int, [c_void_p, ctypes.c_char_p]),
 }
 
 
@@ -229,6 +231,12 @@ class Engine:
 
     def last_launches(self):
         return _L().cgppd_engine_last_launches(self.h)
+
+    def checkpoint(self, path):
+        _ok(_L().cgppd_engine_checkpoint(self.h, str(path).encode()), "checkpoint")
+
+    def restore(self, path):
+        _ok(_L().cgppd_engine_restore(self.h, str(path).encode()), "restore")
 
     def launch_shape(self):
         """(CTAs per replica, threads per CTA, state resident in shared memory)."""

@@ -124,6 +124,17 @@ int cgppd_engine_upload(cgppd_engine *e, int sim, const float *pos4, const float
 int cgppd_engine_download(cgppd_engine *e, int sim, float *pos4, float *rel4, float *centers4, double *potentials,
                           void *stream);
 
+/* Checkpoint and resume.  The reference leaves resuming a stub (src/Simulation.cpp:703-706);
+ * here the complete mutable state of a finalized engine -- coordinates, pair matrices,
+ * internal energies, potentials, temperature ladder and labels, swapped statistics, the
+ * MC step counters that key every replica's Philox stream, exchange bookkeeping, report
+ * rows and surrogate counters -- is written to one file, and restoring it into an engine
+ * built from the same system continues the run exactly as if it had not stopped.
+ * Restore checks the system's shape (simulations, replicas, molecules) and fails on a
+ * mismatch.  Both synchronize the engine's stream first. */
+int cgppd_engine_checkpoint(cgppd_engine *e, const char *path);
+int cgppd_engine_restore(cgppd_engine *e, const char *path);
+
 /* Molecule-pair energies [M*M] and internal energies [M] of one replica. */
 int cgppd_engine_get_matrix(cgppd_engine *e, int sim, int replica, double *E, double *intra);
 
