@@ -408,6 +408,74 @@ __device__ void bonded_terms(const Lists &a, const DevMol &mol, const float4 *p,
     }
 }
 
+// Whether bonded term (kind, k) of a molecule involves residue ri.
+__device__ __forceinline__ bool bonded_has(const Lists &a, const DevMol &mol, int kind, int k, int ri)
+{
+    if (kind == 0) {
+        const int2 b = a.bonds[mol.bond_off + k - a.base[kLBond]];
+        return b.x == ri || b.y == ri;
+    }
+    if (kind == 1) {
+        const int4 an = a.angles[mol.ang_off + k - a.base[kLAng]];
+        return an.x == ri || an.y == ri || an.z == ri;
+    }
+    const int4 tq = a.tors[mol.tor_off + k - a.base[kLTor]];
+    return tq.x == ri || tq.y == ri || tq.z == ri || tq.w == ri;
+}
+
+// Change of the bonded terms that involve residue ri between positions pold and pnew
+// (molecule-relative arrays), thread-strided from t0.
+__device__ void bonded_delta(const Lists &a, const DevMol &mol, const float4 *pnew, const float4 *pold, int ri,
+                             float L, float invL, int t0, int stride, FF &acc)
+{
+    const int nb = mol.nbond, na = mol.nang, nt = mol.ntor;
+    for (int k = t0; k < nb + na + nt; k += stride) {
+        const int kind = (k < nb) ? 0 : (k < nb + na) ? 1 : 2;
+        const int kk = (kind == 0) ? k : (kind == 1) ? k - nb : k - nb - na;
+        if (bonded_has(a, mol, kind, kk, ri))
+            ff_add(acc, bonded_item(a, mol, pnew, L, invL, kind, kk) - bonded_item(a, mol, pold, L, invL, kind, kk));
+    }
+}
+
+// Full internal energy (unexcluded pairs over the molecule's active tiles, indirect
+// subtraction, bonded terms) of a molecule at the state's positions, by one CTA; the
+// same value in every thread.
+__device__ FF intra_full_cta(const Lists &Ls, const DevMol &mol, const float4 *P, const float4 *ST, const int4 *EX,
+                             const float *table, float L, float invL, FF *red)
+{
+    const int t = threadIdx.x, T = blockDim.x, warp = t >> 5, lane = t & 31, NW = T >> 5;
+    const int n = mol.count, st = mol.start;
+    FF acc{0.f, 0.f};
+    for (int k = warp; k < mol.ntile; k += NW) {
+        const int2 tl = Ls.tiles[mol.tile_off + k - Ls.base[kLTile]];
+        const int j = tl.y * 32 + lane;
+        float part = 0.f;
+        if (j < n) {
+            const float4 pj4 = P[st + j], sj = ST[st + j];
+            const float4 pj = make_float4(pj4.x, pj4.y, pj4.z, sj.x);
+            const float2 qj = make_float2(sj.y, sj.z);
+            const int4 ej = EX[st + j];
+            const int iend = (tl.x == tl.y) ? j : min(n, tl.x * 32 + 32);
+            for (int i = tl.x * 32; i < iend; ++i) {
+                if (intra_excluded(EX[st + i], ej))
+                    continue;
+                const float4 pi4 = P[st + i], si = ST[st + i];
+                part += pair_kcal(make_float4(pi4.x, pi4.y, pi4.z, si.x), make_float2(si.y, si.z), pj, qj, table, L,
+                                  invL);
+            }
+        }
+        ff_add(acc, part);
+    }
+    for (int k = t; k < mol.nind; k += T) {
+        const int2 pr = Ls.indsub[mol.ind_off + k - Ls.base[kLInd]];
+        const float4 pa = P[st + pr.x], sa = ST[st + pr.x], pb = P[st + pr.y], sb = ST[st + pr.y];
+        ff_add(acc, -pair_kcal(make_float4(pa.x, pa.y, pa.z, sa.x), make_float2(sa.y, sa.z),
+                               make_float4(pb.x, pb.y, pb.z, sb.x), make_float2(sb.y, sb.z), table, L, invL));
+    }
+    bonded_terms(Ls, mol, P + st, L, invL, t, T, acc);
+    return block_sum_ff_ff(acc, red);
+}
+
 // ------------------------------------------------------------------ move decision
 
 // Loads of mutable state: plain shared-memory loads when resident, L2 loads otherwise
@@ -873,14 +941,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         for (int k = t; k < M * M; k += T)
             EMf[k] = ff_from(__ldcg(&gE[k]));
         __syncthreads();
-        // row sums: S[m] = intra[m] + sum_b E[m][b]
-        for (int k = t; k < M; k += T) {
-            FF v = INTRAf[k];
-            for (int b = 0; b < M; ++b)
-                if (b != k)
-                    ff_add_ff(v, EMf[(long long)k * M + b]);
-            ROWSUMf[k] = v;
-        }
     }
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
     const float tstep = a.tstep[g];
@@ -954,6 +1014,37 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     if (t == 0)
         s_pot = ff_from(__ldcg(&a.potential[g]));
     __syncthreads();
+    if (RES) {
+        // The steps keep flexible molecules' internal energies incrementally (rigid moves
+        // leave them unchanged, local moves add the moved residue's terms), which ignores
+        // the rounding-level changes of rigid moves: re-evaluate them from the state once
+        // per launch and carry the difference into the running total.  Every CTA of the
+        // cluster evaluates the same sums in the same order.
+        if (a.any_flexible)
+            for (int k = 0; k < M; ++k) {
+                if (!(s_mols[k].flags & kMolFlexible))
+                    continue;
+                const FF v = intra_full_cta(Ls, s_mols[k], P, ST, EX, s_table, L, invL, s_red);
+                if (t == 0) {
+                    const FF old = INTRAf[k];
+                    FF pot = s_pot;
+                    ff_add_ff(pot, v);
+                    ff_add_ff(pot, FF{-old.hi, -old.lo});
+                    s_pot = pot;
+                    INTRAf[k] = v;
+                }
+                __syncthreads();
+            }
+        // row sums: S[m] = intra[m] + sum_b E[m][b]
+        for (int k = t; k < M; k += T) {
+            FF v = INTRAf[k];
+            for (int b = 0; b < M; ++b)
+                if (b != k)
+                    ff_add_ff(v, EMf[(long long)k * M + b]);
+            ROWSUMf[k] = v;
+        }
+        __syncthreads();
+    }
     DaView &dv = s_dv;
     if (DA) {
         if (t == 0)
@@ -1175,9 +1266,38 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 s_ej[o - o0] = make_float2(acc.hi, acc.lo);
         }
 
-        // ---- internal energy of a flexible molecule (intra pairs split over the cluster)
+        // ---- internal energy of a flexible molecule (intra pairs split over the cluster).
+        // Resident launches keep it incrementally: rigid moves (rotate, translate) leave it
+        // unchanged, a local move of residue ri adds new - old over ri's unexcluded pairs,
+        // indirect-neighbour corrections and bonded terms (every other term is unchanged
+        // bit for bit); flex moves, and local moves whose centre wraps, recompute it.
         FF iacc{0.f, 0.f};
-        if (flexmol) {
+        const bool incr = RES && flexmol && !nullm &&
+                          (type == kRotate || type == kTranslate || (type == kLocal && !mv.wrapped));
+        if (incr && type == kLocal) {
+            const DevMol &mol = s_mols[m];
+            const int ri = mv.ri;
+            const float4 pn = s_ipos[ri], po4 = P[start + ri];
+            const float4 po = make_float4(po4.x, po4.y, po4.z, pn.w);
+            const float2 qr = s_iq[ri];
+            const int4 er = s_iexcl[ri];
+            for (int j = rank * T + t; j < n; j += C * T) {
+                if (j == ri || intra_excluded(er, s_iexcl[j]))
+                    continue;
+                const float4 pj = s_ipos[j];  // unmoved: the state's position
+                const float2 qj = s_iq[j];
+                ff_add(iacc, pair_kcal(pn, qr, pj, qj, s_table, L, invL) - pair_kcal(po, qr, pj, qj, s_table, L, invL));
+            }
+            for (int k = rank * T + t; k < mol.nind; k += C * T) {
+                const int2 pr = Ls.indsub[mol.ind_off + k - Ls.base[kLInd]];
+                if (pr.x != ri && pr.y != ri)
+                    continue;
+                const int o = (pr.x == ri) ? pr.y : pr.x;
+                ff_add(iacc, pair_kcal(po, qr, s_ipos[o], s_iq[o], s_table, L, invL) -
+                                 pair_kcal(pn, qr, s_ipos[o], s_iq[o], s_table, L, invL));
+            }
+            bonded_delta(Ls, mol, s_ipos, P + start, ri, L, invL, rank * T + t, C * T, iacc);
+        } else if (flexmol && !incr) {
             // the molecule's active 32 x 32 tiles (on and above the diagonal, holding at least
             // one unexcluded pair); when the cluster has spare warps each tile's i range is
             // split into sf chunks (shorter serial chains)
@@ -1309,6 +1429,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                             ff_add_ff(intra_new, rcv[k * M1 + a.max_m]);
                     else
                         intra_new = s_intrap;
+                    if (incr)  // the partials are the change: add the molecule's current value
+                        ff_add_ff(intra_new, INTRAf[m]);
                 }
                 s_intra_new = intra_new;
                 FF new_row = v;
@@ -1356,7 +1478,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 else
                     st.reject++;
                 pairs += (unsigned long long)n * (unsigned long long)(N - n) +
-                         (flexmol ? (unsigned long long)mv.nintra : 0ull);
+                         (flexmol ? (incr ? (type == kLocal ? 2ull * (unsigned long long)(n - 1) : 0ull)
+                                          : (unsigned long long)mv.nintra)
+                                  : 0ull);
                 if (nullm)
                     errbits |= 1u;
             }

@@ -174,6 +174,23 @@ def test_running_total_has_no_drift():
         assert abs(run_tot[r] - ref) <= REL * abs(ref) + 1e-9
 
 
+def test_flexible_running_total_within_bound():
+    # the internal energy of a flexible molecule is kept incrementally between launches
+    # (rigid moves keep it, local moves add the moved residue's terms) and re-evaluated
+    # at every launch: after long blocks the totals stay within 1e-5 of the FP64 energy
+    wl = workloads.make("c1")
+    sim = subset(wl, 4)
+    e = engine_for(wl, [sim], cluster=4)
+    e.run(3, 1000)
+    run_tot = e.replicas(0)["potential"]
+    assert np.allclose(run_tot, e.recompute(False), rtol=1e-5, atol=1e-7)
+    o = oracle_for(wl, sim)
+    for r in range(4):
+        xyz, _, _ = e.state(0, r)
+        e64 = o.energy_of(xyz, oracle.FP64)
+        assert abs(run_tot[r] - e64) <= REL * abs(e64) + 1e-9, (r, run_tot[r], e64)
+
+
 @pytest.mark.parametrize("config", ["c1", "c4"])
 def test_flexible_and_rigid_clusters_match_oracle(config):
     # flexible moves and crankshafts split over a cluster, state resident
