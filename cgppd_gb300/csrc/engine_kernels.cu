@@ -1015,10 +1015,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         s_pot = ff_from(__ldcg(&a.potential[g]));
     __syncthreads();
     if (RES) {
-        // The steps keep flexible molecules' internal energies incrementally (rigid moves
-        // leave them unchanged, local moves add the moved residue's terms), which ignores
-        // the rounding-level changes of rigid moves: re-evaluate them from the state once
-        // per launch and carry the difference into the running total.  Every CTA of the
+        // Local moves keep flexible molecules' internal energies incrementally: re-evaluate
+        // them from the state once per launch (bounding the float-float accumulation of the
+        // increments) and carry the difference into the running total.  Every CTA of the
         // cluster evaluates the same sums in the same order.
         if (a.any_flexible)
             for (int k = 0; k < M; ++k) {
@@ -1267,13 +1266,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         }
 
         // ---- internal energy of a flexible molecule (intra pairs split over the cluster).
-        // Resident launches keep it incrementally: rigid moves (rotate, translate) leave it
-        // unchanged, a local move of residue ri adds new - old over ri's unexcluded pairs,
-        // indirect-neighbour corrections and bonded terms (every other term is unchanged
-        // bit for bit); flex moves, and local moves whose centre wraps, recompute it.
+        // A local move of residue ri (resident launches, centre not wrapped) leaves every
+        // other position bit for bit unchanged, so the new value is the old one plus
+        // new - old over ri's unexcluded pairs, indirect-neighbour corrections and bonded
+        // terms.  Other moves recompute it: a rigid rotation or translation changes the
+        // float positions, and with them the energy, at rounding level, which a running
+        // total must follow to stay within 1e-5 of the energy of its own coordinates.
         FF iacc{0.f, 0.f};
-        const bool incr = RES && flexmol && !nullm &&
-                          (type == kRotate || type == kTranslate || (type == kLocal && !mv.wrapped));
+        const bool incr = RES && flexmol && !nullm && type == kLocal && !mv.wrapped;
         if (incr && type == kLocal) {
             const DevMol &mol = s_mols[m];
             const int ri = mv.ri;
@@ -1478,8 +1478,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 else
                     st.reject++;
                 pairs += (unsigned long long)n * (unsigned long long)(N - n) +
-                         (flexmol ? (incr ? (type == kLocal ? 2ull * (unsigned long long)(n - 1) : 0ull)
-                                          : (unsigned long long)mv.nintra)
+                         (flexmol ? (incr ? 2ull * (unsigned long long)(n - 1) : (unsigned long long)mv.nintra)
                                   : 0ull);
                 if (nullm)
                     errbits |= 1u;

@@ -175,9 +175,9 @@ def test_running_total_has_no_drift():
 
 
 def test_flexible_running_total_within_bound():
-    # the internal energy of a flexible molecule is kept incrementally between launches
-    # (rigid moves keep it, local moves add the moved residue's terms) and re-evaluated
-    # at every launch: after long blocks the totals stay within 1e-5 of the FP64 energy
+    # local moves keep the internal energy of a flexible molecule incrementally (the
+    # moved residue's terms), re-evaluated at every launch: after long blocks the totals
+    # stay within 1e-5 of a fresh evaluation and of the FP64 energy
     wl = workloads.make("c1")
     sim = subset(wl, 4)
     e = engine_for(wl, [sim], cluster=4)
