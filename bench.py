@@ -112,6 +112,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ------------------------------------------------------------------ ranks
+
+def reduce_over_ranks(seconds, counts, dist=None, device="cpu"):
+    """Whole-job figures of a timed region: the slowest rank's time (max over ranks) and
+    the sum of every rank's work; value = summed work / slowest time."""
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    c = torch.tensor([float(x) for x in counts], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(c)
+    return float(t.item()), [float(x) for x in c.tolist()]
+
+
 # ------------------------------------------------------------------ CPU arm
 
 def cpu_port_rate(wl, seconds, threads):
@@ -279,19 +293,11 @@ def gpu_arm(args):
                 launches += e.last_launches()
             ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1)
     steps1, pairs1 = e.counters()
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
-    mc_steps = steps1 - steps0
-    pairs = pairs1 - pairs0
-    tot = torch.tensor([float(mc_steps), float(pairs)], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(tot)
-    value = tot[0].item() / (ms / 1000.0)
-    pair_rate = tot[1].item() / (ms / 1000.0)
+    ms, (all_steps, all_pairs) = reduce_over_ranks(ev0.elapsed_time(ev1), [steps1 - steps0, pairs1 - pairs0],
+                                                   dist, "cuda")
+    value = all_steps / (ms / 1000.0)
+    pair_rate = all_pairs / (ms / 1000.0)
 
     # kernel-level timing of the MC block (the dominant kernel) with events on its stream
     ktimes = []
@@ -337,13 +343,10 @@ def gpu_arm(args):
                 e.download(si, b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(), b[3].data_ptr(), stream=sh)
             stream.synchronize()
         t1 = time.perf_counter()
-        done = e.counters()[0] - s0
         h2d = sum((2 * Rs * N + Rs * M) * 16 for _, N, M, Rs, _ in sims)
         d2h = h2d + sum(Rs * 8 for _, _, _, Rs, _ in sims)
-        tt = torch.tensor([t1 - t0], dtype=torch.float64, device="cuda")
-        if dist:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": done * world / float(tt.item()), "unit": "replica MC steps/s",
+        secs, (done,) = reduce_over_ranks(t1 - t0, [e.counters()[0] - s0], dist, "cuda")
+        e2e = {"value": done / secs, "unit": "replica MC steps/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     cpu = None
