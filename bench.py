@@ -229,6 +229,15 @@ def surrogate_leg(args, torch, flush):
     st = sg.stats(screened, 0)
     d = {k: st[k] - st0.get(k, 0.0) for k in ("proposals", "stage1_reject", "stage2_eval", "stage2_accept")}
     shape = screened.launch_shape()
+    screened.close()
+    # the same with the fallback disabled: what delayed acceptance itself does on this
+    # system (the sampled distribution is exact either way)
+    always = eng.from_workload(wl)
+    sg.attach(always, s, rmse_threshold=1e30)
+    a0 = sg.stats(always, 0)
+    always_rate, always_pairs, _ = timed(always, args.surrogate_blocks)
+    a1 = sg.stats(always, 0)
+    da_always = {k: a1[k] - a0.get(k, 0.0) for k in ("proposals", "stage1_reject", "stage2_eval")}
     out = {"workload": wl.name, "plain_replica_mc_steps_per_s": plain_rate,
            "screened_replica_mc_steps_per_s": da_rate, "speedup": da_rate / plain_rate,
            "exact_pairs_per_step_plain": plain_pairs, "exact_pairs_per_step_screened": da_pairs,
@@ -237,8 +246,12 @@ def surrogate_leg(args, torch, flush):
            "screened_proposals": d["proposals"], "online_rmse_kcal": st["rmse"], "still_screening": bool(st["screening"]),
            "simulations_screened": n_on, "train_samples": s.n_samples, "train_epochs": args.surrogate_epochs,
            "train_seconds_incl_sampling": train_s, "heldout_rmse_per_epoch": [float(x) for x in hist[:, 1]],
-           "cluster_ctas_per_replica": shape[0], "threads_per_cta": shape[1]}
-    screened.close()
+           "cluster_ctas_per_replica": shape[0], "threads_per_cta": shape[1],
+           "no_fallback": {"replica_mc_steps_per_s": always_rate, "speedup": always_rate / plain_rate,
+                           "exact_pairs_per_step": always_pairs,
+                           "stage1_reject_fraction": da_always["stage1_reject"] / max(1.0, da_always["proposals"]),
+                           "online_rmse_kcal": a1["rmse"]}}
+    always.close()
     s.close()
     return out
 

@@ -80,9 +80,9 @@ def subset(wl, nrep):
                                 sim.rotate_steps[:nrep], sim.move_weights, sim.rigid_rotate_prob)
 
 
-def engine_for(wl, sims, cluster=8, threads=256):
+def engine_for(wl, sims, cluster=8, threads=256, resident=True):
     w2 = workloads.Workload(wl.name, sims, wl.lj_raw, wl.torsion_V, wl.torsion_phase, wl.seed)
-    return eng.from_workload(w2, cluster=cluster, threads=threads)
+    return eng.from_workload(w2, cluster=cluster, threads=threads, resident=resident)
 
 
 def oracle_pair_energies(wl, sim, xyz):
@@ -125,8 +125,8 @@ def test_training_samples_match_oracle():
     e.close()
 
 
-def run_pair(wl, nrep, blocks, steps, attach_with=None, **kw):
-    e = engine_for(wl, [subset(wl, nrep)])
+def run_pair(wl, nrep, blocks, steps, attach_with=None, resident=True, **kw):
+    e = engine_for(wl, [subset(wl, nrep)], resident=resident)
     if attach_with is not None:
         assert sg.attach(e, attach_with, **kw) == 1
     e.run(blocks, steps, exchange_after_last=True)
@@ -134,12 +134,14 @@ def run_pair(wl, nrep, blocks, steps, attach_with=None, **kw):
     return e
 
 
-def test_zero_surrogate_reproduces_plain_trajectory():
+@pytest.mark.parametrize("resident", [True, False])
+def test_zero_surrogate_reproduces_plain_trajectory(resident):
     wl = workloads.make("c4")
     s = sg.Surrogate(batch=128, seed=5)
     s.params = np.zeros(sg.N_PARAMS, np.float32)
-    plain = run_pair(wl, 4, 3, 100)
-    da = run_pair(wl, 4, 3, 100, attach_with=s, rmse_threshold=1e9)
+    plain = run_pair(wl, 4, 3, 100, resident=resident)
+    da = run_pair(wl, 4, 3, 100, attach_with=s, resident=resident, rmse_threshold=1e9)
+    assert da.launch_shape()[2] == resident
     rp, rd = plain.replicas(0), da.replicas(0)
     for k in ("accept", "acceptA", "reject", "totalAccept", "totalAcceptReject", "label", "tindex"):
         assert np.array_equal(rp[k], rd[k]), k
