@@ -1208,8 +1208,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         }
 
         // ---- inter-molecule pairs: this CTA's slice of the other residues
+        // the other N - n residues split evenly over the cluster for this move (the
+        // shared-memory slice buffers are sized for the largest system, slice >= sl)
         const int nother = N - n;
-        const int o0 = rank * slice, o1 = min(nother, o0 + slice);
+        const int sl = (nother + C - 1) / C;
+        const int o0 = rank * sl, o1 = min(nother, o0 + sl);
         const int cnt = max(0, o1 - o0);
         // threads per j (each takes every tpj-th i): split the i loop only while the slice
         // leaves threads idle (long per-thread loops keep the 4-way partial sums busy)
