@@ -121,12 +121,14 @@ def compare_runs(e, o, sim_index=0, pos_tol=2e-3, traj_rel=REL):
 # c1 is shorter: its flex moves rotate in float here and in double in the reference loop,
 # so the coordinates drift apart by float rounding and, over a few hundred steps, one
 # Metropolis draw can land inside that rounding of its acceptance probability.
-@pytest.mark.parametrize("config,nrep,blocks,steps", [("c0", 4, 3, 100), ("c4", 4, 2, 60), ("c1", 4, 2, 40)])
+@pytest.mark.parametrize("config,nrep,blocks,steps", [("c0", 4, 3, 100), ("c4", 4, 2, 60), ("c1", 4, 2, 40),
+                                                     ("c2", 3, 2, 20)])
 def test_trajectory_matches_oracle(config, nrep, blocks, steps, resident):
     wl = workloads.make(config)
     sim = subset(wl, nrep)
-    e = engine_for(wl, [sim], resident=resident)
-    assert e.launch_shape()[2] == resident
+    e = engine_for(wl, [sim], cluster=4 if config == "c2" else 1, resident=resident)
+    # C2's replica state (3,518 residues) exceeds the resident budget: always in L2
+    assert e.launch_shape()[2] == (resident and config != "c2")
     o = oracle_for(wl, sim)
     e.run(blocks, steps, exchange_after_last=True)
     orep, oex = o.run(blocks, steps, exchange_after_last=True)
