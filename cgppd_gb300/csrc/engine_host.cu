@@ -602,7 +602,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     base.potential = pot.ptr, base.stats = st.ptr, base.stepc = sc.ptr, base.pairc = pc.ptr, base.errflags = ef.ptr;
     if (e->da)
         base.dastats = das.ptr;
-    const int clusters[5] = {1, 2, 4, 8, 16}, thread_opts[3] = {128, 256, 512};
+    const int clusters[8] = {1, 2, 3, 4, 5, 6, 8, 16}, thread_opts[3] = {128, 256, 512};
     const int steps = 32;
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
@@ -613,7 +613,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     for (int C : clusters) {
         if (fixed_cluster > 0 && C != fixed_cluster)
             continue;
-        if (e->da && C < 4)  // the surrogate's weights are split over 4 or 8 CTAs
+        if (e->da && (C < 4 || 256 % C != 0))  // the surrogate's 256 units split evenly over 4, 8 or 16 CTAs
             continue;
         for (int T : thread_opts) {
             if (fixed_threads > 0 && T != fixed_threads)

@@ -268,12 +268,13 @@ def _tuning(self):
         L.cgppd_engine_tuning.restype = c_int
         L.cgppd_engine_tuning.argtypes = [c_void_p, P(c_int), P(c_int), P(c_int), P(c_float)]
         L._tuning_declared = True
-    n = c_int(16)
-    cl = (c_int * 16)()
-    th = (c_int * 16)()
-    us = (c_float * 16)()
+    cap = 64
+    n = c_int(cap)
+    cl = (c_int * cap)()
+    th = (c_int * cap)()
+    us = (c_float * cap)()
     L.cgppd_engine_tuning(self.h, ctypes.byref(n), cl, th, us)
-    return [(cl[i], th[i], us[i]) for i in range(n.value)]
+    return [(cl[i], th[i], us[i]) for i in range(min(n.value, cap))]
 
 
 Engine.tuning = _tuning

@@ -67,7 +67,7 @@ int cgppd_engine_add_molecule(cgppd_engine *e, int sim, int n, const float *xyz,
 
 /* Build the device tables, upload every replica and compute the initial energies
  * (Simulation::init: initialReplica.E() + internal_molecule_E(true), replicated to
- * every replica).  cluster: CTAs per replica (1, 2, 4, 8, 16); threads per CTA (128, 256,
+ * every replica).  cluster: CTAs per replica (1-8 or 16); threads per CTA (128, 256,
  * 512);
  * 0 for either lets the autotuner pick it from a timed sweep on scratch copies of the
  * state (cached per system shape for the life of the process). */
