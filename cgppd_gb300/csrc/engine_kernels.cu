@@ -1,13 +1,16 @@
 // engine_kernels.cu -- device side of the batched replica-exchange Monte Carlo engine.
 //
-// k_mc<RES>: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
+// k_mc<RES, DA>: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
 // that replica with no inter-replica traffic (replicas are independent between
-// exchanges).  A step restates Replica::MCSearch (src/Replica.cpp:350-414):
-//   1. pick a molecule and a move (src/Molecule.cpp:451-504) from Philox draws,
+// exchanges); every replica of every simulation is in the one launch.  A step restates
+// Replica::MCSearch (src/Replica.cpp:350-414):
+//   1. pick a molecule and a move (src/Molecule.cpp:451-504) from Philox draws (drawn one
+//      step ahead by an idle warp),
 //   2. build the moved molecule's proposed coordinates in shared memory,
 //   3. evaluate the moved molecule against every other residue (its row of the
 //      molecule-pair energy matrix) and, for a flexible molecule, its internal
-//      non-bonded + bonded energy (src/Molecule.cpp:636-699),
+//      non-bonded + bonded energy (src/Molecule.cpp:636-699; a local move evaluates only
+//      the moved residue's terms, every other term being unchanged bit for bit),
 //   4. new total = old total - old row + new row; Metropolis on the float delta with
 //      the float Boltzmann factor, as the reference does (src/Replica.cpp:385-410),
 //   5. on accept, commit coordinates and the row (copy-on-accept; nothing to undo).
@@ -15,19 +18,23 @@
 // change, so the engine evaluates those and keeps the rest in the matrix.
 //
 // RES = true: every CTA copies its replica's state (coordinates, static residue
-// records, centres, pair matrix, row sums) into shared memory at launch, updates it in
-// place, and rank 0 writes it back at the end -- no global-memory latency on the step's
-// serial path.  RES = false (large systems): state stays in global memory (L2) and
-// rank 0 commits there.
+// records, centres, the pair matrix, internal energies and row sums as float-float,
+// and the simulation's static move/bond/tile lists) into shared memory at launch,
+// updates it in place, and rank 0 writes it back at the end -- no global-memory latency
+// and no FP64 arithmetic on the step's serial path.  RES = false (large systems): state
+// stays in global memory (L2) and rank 0 commits there.
 //
 // Within a cluster every CTA builds the same proposal (same draws, same arithmetic),
-// takes a slice of the other residues, and the per-molecule partial rows are summed
-// through distributed shared memory in a fixed rank order, so every CTA takes the same
-// Metropolis decision.
+// takes an even slice of the other residues, and pushes its per-molecule partial rows
+// (float-float) into every CTA's shared memory before one cluster barrier; every CTA sums
+// them in the same rank order, so every CTA takes the same Metropolis decision.
 //
-// k_exchange: one warp per simulation performs the even/odd temperature exchange of
-// Simulation::run (src/Simulation.cpp:770-795) and the per-temperature bookkeeping of
-// Replica::fraction_bound / acceptance_ratio (src/Replica.cpp:1095-1122).
+// DA = true: delayed-acceptance screening with the learned surrogate (see below).
+//
+// k_exchange: one thread per simulation performs the even/odd temperature exchange of
+// Simulation::run (src/Simulation.cpp:770-795), the per-temperature bookkeeping of
+// Replica::fraction_bound / acceptance_ratio (src/Replica.cpp:1095-1122) and the
+// surrogate's fallback check.
 #include <cooperative_groups.h>
 
 #include "cgppd_common.cuh"
