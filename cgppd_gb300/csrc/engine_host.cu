@@ -552,7 +552,7 @@ int cgppd_engine::build()
 // ------------------------------------------------------------------ launch shape
 
 // CTAs per replica C and threads per CTA T; the state is kept in shared memory when the
-// per-CTA footprint stays under 160 KB.
+// per-CTA footprint stays under 210 KB.
 static void configure_shape(cgppd_engine *e, int C, int T)
 {
     e->cluster = C;
@@ -560,7 +560,7 @@ static void configure_shape(cgppd_engine *e, int C, int T)
     const int da = e->da;
     const size_t s_res = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, da, e->lmax);
     const size_t s_da = da ? s_res - engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, 1, e->any_flexible, 0, e->lmax) : 0;
-    e->resident = (e->resident_pref != 0) && s_res <= 160 * 1024 + s_da;
+    e->resident = (e->resident_pref != 0) && s_res <= 210 * 1024 + s_da && s_res <= 226 * 1024;
     e->smem = engine_smem_bytes(e->max_mol, e->max_n, e->max_m, C, e->resident, e->any_flexible, da, e->lmax);
 }
 

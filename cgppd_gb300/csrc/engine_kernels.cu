@@ -107,7 +107,7 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     if (resident) {
         L.P = off;      off += 16 * max_n;
         L.Q = off;      off += 16 * max_n;
-        L.ST = off;     off += 16 * max_n;
+        L.ST = off;     off = align16(off + max_n);  // residue types (sigma/2 in P.w, charge in Q.w)
         L.EX = off;     off += any_flexible ? 16 * max_n : 0;
         L.CEN = off;    off += 16 * max_m;
         L.EM = off;     off = align16(off + 8 * max_m * max_m);
@@ -447,8 +447,8 @@ __device__ void bonded_delta(const Lists &a, const DevMol &mol, const float4 *pn
 // Full internal energy (unexcluded pairs over the molecule's active tiles, indirect
 // subtraction, bonded terms) of a molecule at the state's positions, by one CTA; the
 // same value in every thread.
-__device__ FF intra_full_cta(const Lists &Ls, const DevMol &mol, const float4 *P, const float4 *ST, const int4 *EX,
-                             const float *table, float L, float invL, FF *red)
+__device__ FF intra_full_cta(const Lists &Ls, const DevMol &mol, const float4 *P, const float4 *Q,
+                             const unsigned char *TY, const int4 *EX, const float *table, float L, float invL, FF *red)
 {
     const int t = threadIdx.x, T = blockDim.x, warp = t >> 5, lane = t & 31, NW = T >> 5;
     const int n = mol.count, st = mol.start;
@@ -458,26 +458,24 @@ __device__ FF intra_full_cta(const Lists &Ls, const DevMol &mol, const float4 *P
         const int j = tl.y * 32 + lane;
         float part = 0.f;
         if (j < n) {
-            const float4 pj4 = P[st + j], sj = ST[st + j];
-            const float4 pj = make_float4(pj4.x, pj4.y, pj4.z, sj.x);
-            const float2 qj = make_float2(sj.y, sj.z);
+            const float4 pj = P[st + j];  // resident records: sigma/2 in P.w, charge in Q.w
+            const float2 qj = make_float2(Q[st + j].w, __int_as_float((int)TY[st + j]));
             const int4 ej = EX[st + j];
             const int iend = (tl.x == tl.y) ? j : min(n, tl.x * 32 + 32);
             for (int i = tl.x * 32; i < iend; ++i) {
                 if (intra_excluded(EX[st + i], ej))
                     continue;
-                const float4 pi4 = P[st + i], si = ST[st + i];
-                part += pair_kcal(make_float4(pi4.x, pi4.y, pi4.z, si.x), make_float2(si.y, si.z), pj, qj, table, L,
-                                  invL);
+                part += pair_kcal(P[st + i], make_float2(Q[st + i].w, __int_as_float((int)TY[st + i])), pj, qj, table,
+                                  L, invL);
             }
         }
         ff_add(acc, part);
     }
     for (int k = t; k < mol.nind; k += T) {
         const int2 pr = Ls.indsub[mol.ind_off + k - Ls.base[kLInd]];
-        const float4 pa = P[st + pr.x], sa = ST[st + pr.x], pb = P[st + pr.y], sb = ST[st + pr.y];
-        ff_add(acc, -pair_kcal(make_float4(pa.x, pa.y, pa.z, sa.x), make_float2(sa.y, sa.z),
-                               make_float4(pb.x, pb.y, pb.z, sb.x), make_float2(sb.y, sb.z), table, L, invL));
+        const int ia = st + pr.x, ib = st + pr.y;
+        ff_add(acc, -pair_kcal(P[ia], make_float2(Q[ia].w, __int_as_float((int)TY[ia])), P[ib],
+                               make_float2(Q[ib].w, __int_as_float((int)TY[ib])), table, L, invL));
     }
     bonded_terms(Ls, mol, P + st, L, invL, t, T, acc);
     return block_sum_ff_ff(acc, red);
@@ -915,7 +913,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     // state views: shared-memory copies when resident, global memory otherwise
     float4 *P = RES ? reinterpret_cast<float4 *>(smem + Ly.P) : gP;
     float4 *Q = RES ? reinterpret_cast<float4 *>(smem + Ly.Q) : gQ;
-    const float4 *ST = RES ? reinterpret_cast<const float4 *>(smem + Ly.ST) : gST;
+    // static residue records: global float4 (sigma/2, charge, type, molecule) when not
+    // resident; resident CTAs pack sigma/2 into P.w, the charge into Q.w and the type
+    // into a byte (33 instead of 48 bytes per residue)
+    const float4 *ST = gST;
+    const unsigned char *TY = RES ? reinterpret_cast<const unsigned char *>(smem + Ly.ST) : nullptr;
     const int4 *EX = (RES && a.any_flexible) ? reinterpret_cast<const int4 *>(smem + Ly.EX) : gEX;
     float4 *CEN = RES ? reinterpret_cast<float4 *>(smem + Ly.CEN) : gCEN;
     // resident copies of the pair matrix, internal energies and row sums are float-float
@@ -930,11 +932,12 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         s_mols[k] = a.mols[S.mol_off + k];
     if (RES) {
         float4 *sP = P, *sQ = Q, *sC = CEN;
-        float4 *sST = reinterpret_cast<float4 *>(smem + Ly.ST);
+        unsigned char *sTY = reinterpret_cast<unsigned char *>(smem + Ly.ST);
         for (int i = t; i < N; i += T) {
-            sP[i] = __ldcg(&gP[i]);
-            sQ[i] = __ldcg(&gQ[i]);
-            sST[i] = gST[i];
+            const float4 p = __ldcg(&gP[i]), q = __ldcg(&gQ[i]), sr = gST[i];
+            sP[i] = make_float4(p.x, p.y, p.z, sr.x);
+            sQ[i] = make_float4(q.x, q.y, q.z, sr.y);
+            sTY[i] = (unsigned char)__float_as_int(sr.z);
         }
         if (a.any_flexible) {
             int4 *sEX = reinterpret_cast<int4 *>(smem + Ly.EX);
@@ -1030,7 +1033,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             for (int k = 0; k < M; ++k) {
                 if (!(s_mols[k].flags & kMolFlexible))
                     continue;
-                const FF v = intra_full_cta(Ls, s_mols[k], P, ST, EX, s_table, L, invL, s_red);
+                const FF v = intra_full_cta(Ls, s_mols[k], P, Q, TY, EX, s_table, L, invL, s_red);
                 if (t == 0) {
                     const FF old = INTRAf[k];
                     FF pot = s_pot;
@@ -1131,7 +1134,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         for (int i = t; i < n; i += T) {
             const float4 p = ld_state<RES>(&P[start + i]);
             const float4 q = ld_state<RES>(&Q[start + i]);
-            const float4 sr = ST[start + i];
+            const float4 sr = RES ? make_float4(p.w, q.w, __int_as_float((int)TY[start + i]), 0.f) : ST[start + i];
             s_iq[i] = make_float2(sr.y, sr.z);
             if (flexmol)
                 s_iexcl[i] = EX[start + i];
@@ -1230,10 +1233,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int sub = t & (tpj - 1), jl = t / tpj, jstride = T / tpj;
         // residue record of this thread's next j, loaded one iteration ahead
         float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
+        auto stat_of = [&](int j) -> float4 {
+            return RES ? make_float4(0.f, Q[j].w, __int_as_float((int)TY[j]), 0.f) : ST[j];
+        };
         if (jl < cnt) {
             const int o = o0 + jl, j = (o < start) ? o : o + n;
             npj = ld_state<RES>(&P[j]);
-            nsj = ST[j];
+            nsj = stat_of(j);
         }
         for (int base = 0; base < cnt; base += jstride) {
             const int o = o0 + base + jl;
@@ -1242,11 +1248,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             if (base + jstride + jl < cnt) {
                 const int on = o + jstride, jn = (on < start) ? on : on + n;
                 npj = ld_state<RES>(&P[jn]);
-                nsj = ST[jn];
+                nsj = stat_of(jn);
             }
             FF acc{0.f, 0.f};
             if (valid) {
-                const float4 rj = make_float4(pj.x, pj.y, pj.z, sj.x);
+                const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
                 const float2 qj = make_float2(sj.y, sj.z);
                 // four independent partial sums (instruction-level parallelism), folded
                 // into the float-float accumulator every 32 terms
@@ -1501,10 +1507,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const bool writer = RES || rank == 0;
         if (acc && writer) {
             for (int i = t; i < n; i += T) {
-                float4 p = s_ipos[i];
-                p.w = 0.f;
+                float4 p = s_ipos[i], q = s_irel[i];  // s_ipos.w = sigma/2
+                p.w = RES ? p.w : 0.f;
+                q.w = RES ? s_iq[i].x : 0.f;
                 P[start + i] = p;
-                Q[start + i] = s_irel[i];
+                Q[start + i] = q;
             }
             for (int b = t; b < M; b += T) {
                 if (b != m) {
@@ -1588,8 +1595,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     if (rank == 0) {
         if (RES) {
             for (int i = t; i < N; i += T) {
-                gP[i] = P[i];
-                gQ[i] = Q[i];
+                const float4 p = P[i], q = Q[i];
+                gP[i] = make_float4(p.x, p.y, p.z, 0.f);
+                gQ[i] = make_float4(q.x, q.y, q.z, 0.f);
             }
             for (int k = t; k < M; k += T) {
                 gCEN[k] = CEN[k];
