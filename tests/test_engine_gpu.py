@@ -127,8 +127,7 @@ def test_trajectory_matches_oracle(config, nrep, blocks, steps, resident):
     wl = workloads.make(config)
     sim = subset(wl, nrep)
     e = engine_for(wl, [sim], cluster=4 if config == "c2" else 1, resident=resident)
-    # C2's replica state (3,518 residues) exceeds the resident budget: always in L2
-    assert e.launch_shape()[2] == (resident and config != "c2")
+    assert e.launch_shape()[2] == resident
     o = oracle_for(wl, sim)
     e.run(blocks, steps, exchange_after_last=True)
     orep, oex = o.run(blocks, steps, exchange_after_last=True)
