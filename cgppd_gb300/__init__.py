@@ -34,6 +34,7 @@ _SIGNATURES = {
     "CUDA_EonDevice_async": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_int, c_int, c_int, c_int, c_void_p]),
     "cgppd_last_energy_components": (c_int, [P(c_double)]),
+    "cgppd_set_repulsive_crowding": (c_int, [c_int]),
     "cgppd_get_last_error": (c_int, [c_char_p, c_int]),
     # residue-type tables (include/cgppd_amino_acids.h)
     "cgppd_aminoacids_create": (c_void_p, []),

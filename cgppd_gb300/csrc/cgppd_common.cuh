@@ -28,6 +28,7 @@ constexpr float kKAlpha = 106.4f;
 constexpr float kKBeta = 26.3f;
 constexpr float kPadder = -2.0f;                    // PADDER_IDENTIFIER
 constexpr float kCrowder = -1.0f;                   // CROWDER_IDENTIFIER
+constexpr float kRepulsiveCutoff = 15.0f;           // const_repulsive_cutoff, A
 constexpr float kLog2e = 1.4426950408889634f;
 
 // ------------------------------------------------------------------ float-float sums

@@ -14,6 +14,7 @@
 // is deterministic.  Scratch (partials + ticket + result) is per (device, stream),
 // allocated on first use and reused.
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -32,6 +33,9 @@ constexpr int kTile = 128;
 constexpr int kWarps = kTile / 32;
 
 __constant__ float c_boxdim;  // CUDA_setBoxDimension, module state per device
+// cgppd_set_repulsive_crowding: the reference's compile-time REPULSIVE_CROWDING
+// (src/definitions.h:18) as process-wide module state, read at each launch
+std::atomic<int> g_repulsive_crowding{0};
 
 struct Scratch {
     unsigned *ticket = nullptr;   // CTA completion counter, self-resetting
@@ -56,7 +60,7 @@ __global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict_
                                                        int P, int nt, const float *__restrict__ lj_raw,
                                                        double *__restrict__ partials, unsigned *__restrict__ ticket,
                                                        unsigned *__restrict__ flags, double *__restrict__ result,
-                                                       float *__restrict__ async_out, int async_count)
+                                                       float *__restrict__ async_out, int async_count, int rc)
 {
     __shared__ float4 s_pos[kTile];
     __shared__ float4 s_meta[kTile];
@@ -95,6 +99,7 @@ __global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict_
         const float ybond = frac_int(py.w, ydom);
         const float ychain = frac_int(my.w, ymol);
         const bool diag = (tx == ty);
+        const bool ycrowd = rc && (my.w == kCrowder);
         for (int jb = 0; jb < kTile; jb += 32) {
             float lj_t = 0.f, dh_t = 0.f;
 #pragma unroll 4
@@ -119,15 +124,24 @@ __global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict_
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float inv_r = rsqrt_refined(r2);
                     const float r = r2 * inv_r;
-                    int idx = __float2int_rn(20.0f * my.x + mx.x);
-                    if ((unsigned)idx >= 400u) {
-                        bad = 1u;
-                        idx = 0;
+                    if (ycrowd || (rc && mx.w == kCrowder)) {
+                        // REPULSIVE_CROWDING (src/CudaFunctions.cu:335-338, :492-498):
+                        // (6/r)^12 in RT units below 15 A, no Debye-Hueckel term
+                        if (r < kRepulsiveCutoff) {
+                            const float sc = 6.0f * inv_r, s2 = sc * sc, s6 = s2 * s2 * s2;
+                            lj_t += s6 * s6;
+                        }
+                    } else {
+                        int idx = __float2int_rn(20.0f * my.x + mx.x);
+                        if ((unsigned)idx >= 400u) {
+                            bad = 1u;
+                            idx = 0;
+                        }
+                        const float eij = s_eij[idx];
+                        const float sig = (my.z + mx.z) * 0.5f;
+                        lj_t += lj_term(eij, sig, inv_r * inv_r);
+                        dh_t += dh_term(my.y * mx.y, r, inv_r);
                     }
-                    const float eij = s_eij[idx];
-                    const float sig = (my.z + mx.z) * 0.5f;
-                    lj_t += lj_term(eij, sig, inv_r * inv_r);
-                    dh_t += dh_term(my.y * mx.y, r, inv_r);
                 }
             }
             ff_add(lj, lj_t);
@@ -245,12 +259,13 @@ int launch_energy(bool nc, const float4 *pos, const float4 *meta, int P, const f
 {
     const int nt = (P + kTile - 1) / kTile;
     const int blocks = nt * (nt + 1) / 2;
+    const int rc = g_repulsive_crowding.load();
     if (nc)
         k_tile_energy<true><<<blocks, kTile, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket, s->flags,
-                                                           s->result, async_out, async_count);
+                                                           s->result, async_out, async_count, rc);
     else
         k_tile_energy<false><<<blocks, kTile, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket, s->flags,
-                                                            s->result, async_out, async_count);
+                                                            s->result, async_out, async_count, rc);
     return cgppd_check(cudaGetLastError(), "energy kernel launch");
 }
 
@@ -389,6 +404,16 @@ void CUDA_EonDevice_async(float4 *residuePositions, float4 *residueMeta, int *re
         return;
     launch_energy(false, residuePositions, residueMeta, datasetSize, table, s, device_result,
                   resultSize * resultSize, stream);
+}
+
+// The reference selects the crowder potential at compile time (REPULSIVE_CROWDING,
+// src/definitions.h:18; off in its default build); this library selects it at run
+// time for every later energy call of the process: 0 (default) the full potential for
+// crowder pairs, 1 the repulsive (6/r)^12 term below 15 A without Debye-Hueckel.
+// Returns the previous setting.
+int cgppd_set_repulsive_crowding(int on)
+{
+    return g_repulsive_crowding.exchange(on ? 1 : 0);
 }
 
 // Components of the last synchronous call on the current device (LJ raw, DH raw,

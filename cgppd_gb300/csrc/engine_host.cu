@@ -467,6 +467,22 @@ int cgppd_engine::build()
             lmax[k] = std::max(lmax[k], ds.lcount[k]);
         }
         ds.non_crowders = non_crowders;
+        ds.crowd_start = -1;
+        if (hs.p.repulsive_crowding) {
+            // crowders after every other molecule (the argfile's `crowders` section follows
+            // its `files`) and rigid: a crowder pair is then j >= crowd_start or a crowder mover
+            int first = 0;
+            for (int mi = 0; mi < non_crowders; ++mi)
+                first += hs.mols[mi].n;
+            for (int mi = non_crowders; mi < M; ++mi) {
+                const HostMolecule &hm = hs.mols[mi];
+                if (!hm.crowder)
+                    return cgppd_fail("engine: repulsive crowding needs the crowders after every other molecule");
+                if (!hs.p.rigid_only && (hm.all_flexible || !hm.segments.empty()))
+                    return cgppd_fail("engine: repulsive crowding needs rigid crowders");
+            }
+            ds.crowd_start = first;
+        }
         // Replica::sample chooses what the bound test compares (src/Replica.cpp:1043-1075)
         if (M == 1)
             ds.nc_mode = 0;
@@ -603,7 +619,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     if (e->da)
         base.dastats = das.ptr;
     const int clusters[8] = {1, 2, 3, 4, 5, 6, 8, 16}, thread_opts[3] = {128, 256, 512};
-    const int steps = 32;
+    const int steps = 16;
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -628,16 +644,37 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
                 cudaGetLastError();  // a shape the device cannot schedule: skip it
                 continue;
             }
-            cudaEventRecord(ev0, e->own_stream);
-            cudaError_t err = launch_mc_block(a, e->total_replicas, steps, T, e->smem, e->own_stream);
-            cudaEventRecord(ev1, e->own_stream);
-            if (err != cudaSuccess || cudaEventSynchronize(ev1) != cudaSuccess) {
-                cudaGetLastError();
+            // the marginal cost of a step: launches of n and 2n steps (n sized so that one
+            // takes about 1 ms after a short probe), each the faster of two, differenced so
+            // that the per-launch set-up (state load and write-back) drops out
+            auto time_launch = [&](int n_steps, float &ms_out) -> bool {
+                cudaEventRecord(ev0, e->own_stream);
+                cudaError_t err = launch_mc_block(a, e->total_replicas, n_steps, T, e->smem, e->own_stream);
+                cudaEventRecord(ev1, e->own_stream);
+                if (err != cudaSuccess || cudaEventSynchronize(ev1) != cudaSuccess) {
+                    cudaGetLastError();
+                    return false;
+                }
+                cudaEventElapsedTime(&ms_out, ev0, ev1);
+                return true;
+            };
+            float probe = 0.f;
+            if (!time_launch(steps, probe))
                 continue;
+            const float probe_us = 1000.f * probe / steps;
+            const int n = std::max(steps, std::min(1024, (int)(1000.f / std::max(probe_us, 1e-3f))));
+            float t1 = 1e30f, t2 = 1e30f;
+            bool ok = true;
+            for (int rep = 0; rep < 2 && ok; ++rep) {
+                float u = 0.f, v = 0.f;
+                ok = time_launch(n, u) && time_launch(2 * n, v);
+                t1 = std::min(t1, u);
+                t2 = std::min(t2, v);
             }
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, ev0, ev1);
-            const float us = 1000.f * ms / steps;
+            if (!ok)
+                continue;
+            // (a difference swamped by noise falls back to the plain per-step time)
+            const float us = (t2 > t1) ? 1000.f * (t2 - t1) / n : 1000.f * t2 / (2 * n);
             e->tuning.push_back({C, T, us});
             if (us < best * 0.97f) {  // prefer the smaller shape unless clearly faster
                 best = us;

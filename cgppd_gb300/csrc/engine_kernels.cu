@@ -82,6 +82,29 @@ __host__ __device__ inline int da_rows(int max_m) { return (((max_m - 1 > 1 ? ma
 
 __host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
 
+// Lanes per other residue j in the inter-pair loop of a move of an n-residue molecule
+// (N residues in the simulation, C CTAs of W warps): g lanes share one j and take every
+// g-th residue i of the mover, a warp holds floor(32 / g) such groups.  Cost of the busiest
+// thread: passes over the CTA's slice x (ceil(n / g) pairs + a per-j overhead for the
+// loads and the log2(g)-step reduction); the cheapest g wins, ties to the smaller g.
+__host__ __device__ inline int pair_lanes(int n, int N, int C, int W) {
+    const int sl = (N - n + C - 1) / C;
+    int best = 1, best_cost = 0x7fffffff;
+    for (int g = 1; g <= 32 && g <= (n > 1 ? n : 1); ++g) {
+        const int per = W * (32 / g);
+        const int passes = (sl + per - 1) / per;
+        int lg = 0;
+        while ((1 << lg) < g)
+            ++lg;
+        const int cost = passes * ((n + g - 1) / g + 2 + lg);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = g;
+        }
+    }
+    return best;
+}
+
 enum ListId { kLBond = 0, kLAng, kLTor, kLInd, kLFlex, kLFopt, kLBranch, kLLocal, kLCrank, kLTile };
 constexpr int kNumLists = 10;
 
@@ -336,6 +359,23 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
     if (m4e < 0.0f && s6 > 0.5f)
         u = fmaf(-0.5f, m4e, -u);
     return u + qa.x * qb.x * ex2_sfu(r * (-kLog2e / kXi)) * inv_r;
+}
+
+// Repulsive crowder pair in kcal/mol, the reference's REPULSIVE_CROWDING build
+// (src/Replica.cpp:416-419 and :434-472, src/CudaFunctions.cu:335-338 and :492-498):
+// (6/r)^12 RT below const_repulsive_cutoff (15 A, src/definitions.h:38), zero beyond,
+// and no Debye-Hueckel term.
+__device__ __forceinline__ float crowder_kcal(float4 a, float4 b, float L, float invL)
+{
+    const float dx = min_image(a.x - b.x, L, invL);
+    const float dy = min_image(a.y - b.y, L, invL);
+    const float dz = min_image(a.z - b.z, L, invL);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float inv_r = rsqrt_refined(r2);
+    const float s = 6.0f * inv_r;
+    const float s2 = s * s;
+    const float s6 = s2 * s2 * s2;
+    return (r2 * inv_r < kRepulsiveCutoff) ? kRTtoKcal * (s6 * s6) : 0.0f;
 }
 
 __device__ __forceinline__ bool intra_excluded(int4 ei, int4 ej)
@@ -928,8 +968,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 
     for (int k = t; k < kTableStride * kTableStride; k += T)
         s_table[k] = a.table[k];
-    for (int k = t; k < M; k += T)
-        s_mols[k] = a.mols[S.mol_off + k];
+    for (int k = t; k < M; k += T) {
+        DevMol mk = a.mols[S.mol_off + k];
+        mk.pair_lanes = pair_lanes(mk.count, N, C, NW);
+        s_mols[k] = mk;
+    }
     if (RES) {
         float4 *sP = P, *sQ = Q, *sC = CEN;
         unsigned char *sTY = reinterpret_cast<unsigned char *>(smem + Ly.ST);
@@ -1224,58 +1267,77 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int sl = (nother + C - 1) / C;
         const int o0 = rank * sl, o1 = min(nother, o0 + sl);
         const int cnt = max(0, o1 - o0);
-        // threads per j (each takes every tpj-th i): split the i loop only while the slice
-        // leaves threads idle (long per-thread loops keep the 4-way partial sums busy)
-        int tpj = 1;
-        if (cnt > 0)
-            while (tpj < 32 && cnt * tpj * 2 <= T)
-                tpj <<= 1;
-        const int sub = t & (tpj - 1), jl = t / tpj, jstride = T / tpj;
+        // g lanes per j (each takes every g-th i), floor(32 / g) groups of lanes per warp;
+        // the lanes past the last whole group idle
+        const int g = s_mols[m].pair_lanes, jw = 32 / g;
+        // repulsive crowding: pairs with a crowder (j >= cstart, or a crowder mover) take
+        // the crowder term
+        const int cstart = (S.crowd_start >= 0) ? S.crowd_start : 0x7fffffff;
+        const bool mcrowd = S.crowd_start >= 0 && m >= S.non_crowders;
+        const int sub = lane % g, grp = lane / g;
+        const int jl = warp * jw + grp, jstride = NW * jw;
+        const bool lane_on = grp < jw;
         // residue record of this thread's next j, loaded one iteration ahead
         float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
         auto stat_of = [&](int j) -> float4 {
             return RES ? make_float4(0.f, Q[j].w, __int_as_float((int)TY[j]), 0.f) : ST[j];
         };
-        if (jl < cnt) {
+        if (lane_on && jl < cnt) {
             const int o = o0 + jl, j = (o < start) ? o : o + n;
             npj = ld_state<RES>(&P[j]);
             nsj = stat_of(j);
         }
         for (int base = 0; base < cnt; base += jstride) {
             const int o = o0 + base + jl;
-            const bool valid = (base + jl) < cnt;
+            const bool valid = lane_on && (base + jl) < cnt;
+            const bool crowd = mcrowd || ((o < start) ? o : o + n) >= cstart;
             const float4 pj = npj, sj = nsj;
-            if (base + jstride + jl < cnt) {
+            if (lane_on && base + jstride + jl < cnt) {
                 const int on = o + jstride, jn = (on < start) ? on : on + n;
                 npj = ld_state<RES>(&P[jn]);
                 nsj = stat_of(jn);
             }
             FF acc{0.f, 0.f};
-            if (valid) {
+            if (valid && crowd) {
+                float p0 = 0.f;
+                int cntp = 0;
+                for (int i = sub; i < n; i += g) {
+                    p0 += crowder_kcal(s_ipos[i], pj, L, invL);
+                    if (++cntp == 32) {
+                        ff_add(acc, p0);
+                        p0 = 0.f;
+                        cntp = 0;
+                    }
+                }
+                ff_add(acc, p0);
+            } else if (valid) {
                 const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
                 const float2 qj = make_float2(sj.y, sj.z);
                 // four independent partial sums (instruction-level parallelism), folded
                 // into the float-float accumulator every 32 terms
                 float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
                 int i = sub, cntp = 0;
-                for (; i + 3 * tpj < n; i += 4 * tpj) {
+                for (; i + 3 * g < n; i += 4 * g) {
                     p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
-                    p1 += pair_kcal(s_ipos[i + tpj], s_iq[i + tpj], rj, qj, s_table, L, invL);
-                    p2 += pair_kcal(s_ipos[i + 2 * tpj], s_iq[i + 2 * tpj], rj, qj, s_table, L, invL);
-                    p3 += pair_kcal(s_ipos[i + 3 * tpj], s_iq[i + 3 * tpj], rj, qj, s_table, L, invL);
+                    p1 += pair_kcal(s_ipos[i + g], s_iq[i + g], rj, qj, s_table, L, invL);
+                    p2 += pair_kcal(s_ipos[i + 2 * g], s_iq[i + 2 * g], rj, qj, s_table, L, invL);
+                    p3 += pair_kcal(s_ipos[i + 3 * g], s_iq[i + 3 * g], rj, qj, s_table, L, invL);
                     if (++cntp == 8) {
                         ff_add(acc, (p0 + p1) + (p2 + p3));
                         p0 = p1 = p2 = p3 = 0.f;
                         cntp = 0;
                     }
                 }
-                for (; i < n; i += tpj)
+                for (; i < n; i += g)
                     p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
                 ff_add(acc, (p0 + p1) + (p2 + p3));
             }
-            for (int o2 = 1; o2 < tpj; o2 <<= 1) {
-                FF w{__shfl_xor_sync(0xffffffffu, acc.hi, o2), __shfl_xor_sync(0xffffffffu, acc.lo, o2)};
-                ff_add_ff(acc, w);
+            // segmented tree sum towards the group's first lane: after the step with offset
+            // d, lane sub holds the lanes [sub, min(sub + 2d, g)) of its group
+            for (int d = 1; d < g; d <<= 1) {
+                const FF w{__shfl_down_sync(0xffffffffu, acc.hi, d), __shfl_down_sync(0xffffffffu, acc.lo, d)};
+                if (sub + d < g)
+                    ff_add_ff(acc, w);
             }
             if (valid && sub == 0)
                 s_ej[o - o0] = make_float2(acc.hi, acc.lo);
@@ -1657,6 +1719,7 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
     double *E = a.emat + S.emat_off + (long long)r * M * M;
     for (int b = am + 1; b < M; ++b) {
         const DevMol mb = a.mols[S.mol_off + b];
+        const bool crowd = S.crowd_start >= 0 && (am >= S.non_crowders || b >= S.non_crowders);
         FF acc{0.f, 0.f};
         for (int jj = t; jj < mb.count; jj += T) {
             const int j = mb.start + jj;
@@ -1666,7 +1729,8 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
             const float2 qj = make_float2(sj.y, sj.z);
             float part = 0.f;
             for (int i = 0; i < n; ++i) {
-                part += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                part += crowd ? crowder_kcal(s_ipos[i], rj, L, invL)
+                              : pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
                 if ((i & 31) == 31) {
                     ff_add(acc, part);
                     part = 0.f;
@@ -1751,12 +1815,12 @@ __device__ void report_slot(ReplicaStats &s, float4 &out)
 }
 
 // One warp per simulation: the per-temperature report (once sampling has started),
-// then the even/odd exchange sweep.
+// then the even/odd exchange sweep.  Lanes take temperatures (report) and neighbour
+// pairs (exchange) in parallel: the pairs of one sweep are disjoint, so every swap
+// touches its own two slots.
 __global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block)
 {
-    const int s = blockIdx.x;
-    if (threadIdx.x != 0)
-        return;
+    const int s = blockIdx.x, lane = threadIdx.x;
     const DevSim S = a.sims[s];
     int *st = a.sim_state + 4 * s;
     const int x = st[1];
@@ -1766,28 +1830,33 @@ __global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block
     if (a.da && a.sim_da[s]) {
         double e2 = 0.0;
         unsigned long long cnt = 0;
-        for (int k = 0; k < R; ++k) {
+        for (int k = lane; k < R; k += 32) {
             DAStats &d = a.dastats[S.rep_off + k];
             e2 += d.win_e2;
             cnt += d.win_n;
             d.win_e2 = 0.0;
             d.win_n = 0;
         }
-        if (cnt >= (unsigned long long)a.sur_min && e2 > (double)a.sur_thr2 * (double)cnt)
+        for (int o = 16; o > 0; o >>= 1) {
+            e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0 && cnt >= (unsigned long long)a.sur_min && e2 > (double)a.sur_thr2 * (double)cnt)
             a.sim_da[s] = 0;
     }
     // reporting happens when sampling has started (src/Simulation.cpp:751-768)
     if ((long long)steps_per_block * x >= (long long)S.sample_after && x < a.report_capacity) {
-        for (int tt = 0; tt < R; ++tt) {
+        for (int tt = lane; tt < R; tt += 32) {
             const int slot = a.slot_of_t[S.rep_off + tt];
             float4 o;
             report_slot(a.stats[S.rep_off + slot], o);
             a.report[(long long)x * total_replicas + S.rep_off + tt] = o;
         }
     }
+    __syncwarp();  // the sweep swaps statistics the report has just updated
     int exchanges = 0, tests = 0;
     const int offset = st[0];
-    for (int ti = offset; ti < R - 1; ti += 2) {
+    for (int ti = offset + 2 * lane; ti < R - 1; ti += 64) {
         const int i = a.slot_of_t[S.rep_off + ti], j = a.slot_of_t[S.rep_off + ti + 1];
         const int gi = S.rep_off + i, gj = S.rep_off + j;
         const double Ti = a.temperature[gi], Tj = a.temperature[gj];
@@ -1815,22 +1884,24 @@ __global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block
         }
         ++tests;
     }
-    st[0] = 1 - offset;
-    if (x < a.report_capacity)
-        a.exch_report[(long long)x * gridDim.x + s] = make_int2(exchanges, tests);
-    st[2] += exchanges;
-    st[3] += tests;
-    st[1] = x + 1;
+    exchanges = __reduce_add_sync(0xffffffffu, exchanges);
+    tests = __reduce_add_sync(0xffffffffu, tests);
+    if (lane == 0) {
+        st[0] = 1 - offset;
+        if (x < a.report_capacity)
+            a.exch_report[(long long)x * gridDim.x + s] = make_int2(exchanges, tests);
+        st[2] += exchanges;
+        st[3] += tests;
+        st[1] = x + 1;
+    }
 }
 
 // Final per-temperature report after the last block (src/Simulation.cpp:834-848).
 __global__ void k_final_report(EngineArgs a, int total_replicas, int row)
 {
     const int s = blockIdx.x;
-    if (threadIdx.x != 0)
-        return;
     const DevSim S = a.sims[s];
-    for (int tt = 0; tt < S.R; ++tt) {
+    for (int tt = threadIdx.x; tt < S.R; tt += blockDim.x) {
         const int slot = a.slot_of_t[S.rep_off + tt];
         float4 o;
         report_slot(a.stats[S.rep_off + slot], o);

@@ -40,7 +40,8 @@ struct DevSim {
     int sample_freq, sample_after;
     float bound_threshold;       // kcal/mol, BOUND_ENERGY_VALUE
     int max_mol;                 // largest molecule
-    int pad0;
+    int crowd_start;             // repulsive crowding: first residue of the trailing crowders
+                                 // (their pairs use (6/r)^12 RT below 15 A, no DH); -1: off
     // The same choices as integer thresholds on the raw 32-bit draw w (u = w / 2^32):
     // u < c  <=>  w < ceil(c * 2^32), so the comparisons are exact without FP64.
     unsigned long long thr4[4];  // cumulative weights, flexible molecule
@@ -65,6 +66,7 @@ struct DevMol {
     int fr0, fr1, fr2;           // residues (molecule-relative) spanning the body frame
     int tile_off, ntile;         // 32 x 32 intra tiles (ta <= tb) holding an unexcluded pair
     float tors_const;            // sum of V_n over the molecule's torsions (kcal/mol)
+    int pair_lanes;              // lanes per other residue in the inter pair loop (set per launch)
 };
 
 // Delayed-acceptance counters of one replica slot (not swapped on exchange).

@@ -234,6 +234,7 @@ void Simulation::loadArgsFromFile()
                     parameters.moveWeights[k] = (float)std::atof(w[1 + k].c_str());
             } else if (key == "seed") parameters.seed = std::strtoull(v, nullptr, 10);
             else if (key == "datadir") parameters.dataDir = v;
+            else if (key == "repulsivecrowding") parameters.repulsiveCrowding = std::atoi(v) != 0;
             else std::fprintf(stderr, "cgppd: unknown parameter: %s\n", key.c_str());
         }
     }
@@ -356,6 +357,7 @@ void Simulation::init(int argc, char **argv, int pid)
     p.sample_frequency = parameters.sampleFrequency;
     p.sample_after = parameters.sampleStartsAfter;
     p.bound_threshold = kBoundEnergy;
+    p.repulsive_crowding = parameters.repulsiveCrowding ? 1 : 0;
     if (cgppd_engine_add_simulation(engine_, &p) < 0)
         throw "Engine set-up failed.";
     for (size_t k = 0; k < molecules.size(); ++k) {
@@ -557,7 +559,7 @@ extern "C" int cgppd_args_dump(int argc, char **argv, int mode, char *buf, int b
       << "\nnonCrowders=" << p.nonCrowders << "\npid=" << p.pid << "\nresume=" << p.resume << "\nbound=" << p.bound
       << "\ntemperatureMin=" << p.temperatureMin << "\ntemperatureMax=" << p.temperatureMax << "\nprefix=" << p.prefix
       << "\nfile=" << p.file << "\ntitle=" << p.title << "\nmolecules=" << p.mdata.size()
-      << "\nnamed=" << p.mdata_map.size() << "\n";
+      << "\nnamed=" << p.mdata_map.size() << "\nrepulsiveCrowding=" << p.repulsiveCrowding << "\n";
     for (size_t i = 0; i < p.mdata.size(); ++i) {
         const cgppd::MolData &m = p.mdata[i];
         o << "mol" << i << "=" << m.pdbfilename << " " << (m.name.empty() ? "-" : m.name) << " " << m.translate << " "

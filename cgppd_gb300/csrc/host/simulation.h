@@ -56,6 +56,7 @@ struct ArgData {
     float moveWeights[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     unsigned long long seed = 0;  // 0: from the clock, as the reference seeds its RNGs
     std::string dataDir = "data";
+    bool repulsiveCrowding = false;  // REPULSIVE_CROWDING (src/definitions.h:18), off there
 };
 
 class Simulation {

@@ -16,7 +16,7 @@ class SimParams(ctypes.Structure):
     _fields_ = [("n_replicas", c_int), ("box", c_float), ("temperatures", P(c_float)),
                 ("translate_steps", P(c_float)), ("rotate_steps", P(c_double)), ("move_weights", c_float * 4),
                 ("rigid_rotate_prob", c_float), ("sample_frequency", c_int), ("sample_after", c_int),
-                ("bound_threshold", c_float), ("rigid_only", c_int)]
+                ("bound_threshold", c_float), ("rigid_only", c_int), ("repulsive_crowding", c_int)]
 
 
 _DECL = {
@@ -107,13 +107,14 @@ class Engine:
 
     def add_simulation(self, temperatures, translate_steps, rotate_steps, box, move_weights=(1, 1, 1, 1),
                        rigid_rotate_prob=0.5, sample_frequency=0, sample_after=0, bound_threshold=-1.1844,
-                       rigid_only=False):
+                       rigid_only=False, repulsive_crowding=False):
         T = np.ascontiguousarray(temperatures, np.float32)
         ts = np.ascontiguousarray(translate_steps, np.float32)
         rs = np.ascontiguousarray(rotate_steps, np.float64)
         p = SimParams(len(T), float(box), _p(T, c_float), _p(ts, c_float), _p(rs, c_double),
                       (c_float * 4)(*move_weights), float(rigid_rotate_prob), int(sample_frequency),
-                      int(sample_after), float(bound_threshold), int(bool(rigid_only)))
+                      int(sample_after), float(bound_threshold), int(bool(rigid_only)),
+                      int(bool(repulsive_crowding)))
         sim = _ok(_L().cgppd_engine_add_simulation(self.h, ctypes.byref(p)), "add_simulation")
         self.sims.append(len(T))
         return sim
@@ -251,7 +252,8 @@ def from_workload(wl, cluster=0, threads=0, seed=None, sample_frequency=0, sampl
     e = Engine(wl.lj_raw, wl.torsion_V, wl.torsion_phase, seed=wl.seed if seed is None else seed)
     for sim in wl.sims:
         s = e.add_simulation(sim.temperatures, sim.translate_steps, sim.rotate_steps, sim.box, sim.move_weights,
-                             sim.rigid_rotate_prob, sample_frequency, sample_after)
+                             sim.rigid_rotate_prob, sample_frequency, sample_after,
+                             repulsive_crowding=getattr(sim, "repulsive_crowding", False))
         for m in sim.molecules:
             e.add_molecule(s, m.xyz, m.types, m.charges, m.radii, chain_ids=m.chain_ids, res_seq=m.res_seq,
                            chain_index=m.chain_index, all_flexible=m.all_flexible, crowder=m.crowder,

@@ -54,8 +54,9 @@ class Molecule:
 
 class Simulation:
     def __init__(self, molecules, box, temperatures, translate_steps, rotate_steps, move_weights=(1, 1, 1, 1),
-                 rigid_rotate_prob=0.5):
+                 rigid_rotate_prob=0.5, repulsive_crowding=False):
         self.molecules = molecules
+        self.repulsive_crowding = bool(repulsive_crowding)
         self.box = float(box)
         self.temperatures = np.ascontiguousarray(temperatures, np.float32)
         self.translate_steps = np.ascontiguousarray(translate_steps, np.float32)

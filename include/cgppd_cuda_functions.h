@@ -81,6 +81,14 @@ void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *
  * synchronous call on the current device.  Returns 0 on success. */
 int cgppd_last_energy_components(double *out3);
 
+/* Run-time form of the reference's compile-time REPULSIVE_CROWDING switch
+ * (src/definitions.h:18, off in its default build; src/CudaFunctions.cu:335-338 and
+ * :492-498): when on, every pair with a crowder residue (meta.w == -1) contributes
+ * (6/r)^12 in RT units below 15 A and no Debye-Hueckel term, in every later energy
+ * call of the process (CUDA_EonDevice, _async, _noalloc).  Returns the previous
+ * setting (0 off, 1 on). */
+int cgppd_set_repulsive_crowding(int on);
+
 /* Library extension: the calling thread's last error code (0 = none) and message;
  * clears it. */
 int cgppd_get_last_error(char *buf, int buflen);

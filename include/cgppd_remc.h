@@ -38,6 +38,12 @@ typedef struct cgppd_sim_params {
     float bound_threshold;        /* kcal/mol (-1.1844, src/definitions.h:33) */
     int rigid_only;               /* treat flexible molecules as rigid
                                      (Replica::calculate_rigid_potential_only) */
+    int repulsive_crowding;       /* pairs with a crowder residue: u = (6/r)^12 RT for
+                                     r < 15 A and no Debye-Hueckel term, the reference's
+                                     REPULSIVE_CROWDING build (src/Replica.cpp:416-472,
+                                     src/definitions.h:18,38); 0 = the full potential.
+                                     Crowders must then follow every other molecule and
+                                     be rigid. */
 } cgppd_sim_params;
 
 /* Replaces the parameter set-up of Simulation::init (src/Simulation.cpp:553) and

@@ -49,6 +49,11 @@ def lib():
         L.oracle_E_intra.argtypes = [c_int, c_int, f32p, i32p, f32p, f32p, i32p, c_int, i32p, c_int, i32p, c_int,
                                      i32p, c_int, i32p, f64p, f64p, c_int, f32p, c_int, c_float, c_int, f64p]
         L.oracle_E_packed.argtypes = [c_int, c_int, c_int, f32p, f32p, f32p, c_float, f64p]
+        L.oracle_E_packed_rc.argtypes = [c_int, c_int, c_int, c_int, f32p, f32p, f32p, c_float, f64p]
+        L.oracle_E_inter_matrix_rc.argtypes = [c_int, c_int, i32p, i32p, i32p, f32p, i32p, f32p, f32p, f32p, c_int,
+                                               c_float, f64p]
+        L.or_crowder_term.argtypes = [c_int, ctypes.c_double]
+        L.or_crowder_term.restype = ctypes.c_double
         L.oracle_total.argtypes = [f64p, c_int]
         L.oracle_total.restype = ctypes.c_double
         L.oracle_philox4x32_10.argtypes = [u32p, u32p, u32p]
@@ -346,6 +351,25 @@ def E_inter_matrix(mode, xyz, aa, q, s, start, cnt, table, box):
     return out.reshape(M, M)
 
 
+def E_inter_matrix_rc(mode, xyz, aa, q, s, start, cnt, crowder, table, box):
+    """E_inter_matrix under repulsive crowding (crowder: per-molecule flags)."""
+    t = np.ascontiguousarray(np.asarray(table, np.float32).reshape(-1))
+    nt = int(round(math.sqrt(t.size)))
+    M = len(start)
+    out = np.zeros(M * M, np.float64)
+    lib().oracle_E_inter_matrix_rc(mode, M, np.ascontiguousarray(start, np.int32),
+                                   np.ascontiguousarray(cnt, np.int32), np.ascontiguousarray(crowder, np.int32),
+                                   np.ascontiguousarray(xyz, np.float32).reshape(-1),
+                                   np.ascontiguousarray(aa, np.int32), np.ascontiguousarray(q, np.float32),
+                                   np.ascontiguousarray(s, np.float32), t, nt, float(box), out)
+    return out.reshape(M, M)
+
+
+def crowder_term(mode, r):
+    """Repulsive crowder pair term in RT units (REPULSIVE_CROWDING builds)."""
+    return lib().or_crowder_term(mode, float(r))
+
+
 def intra_inputs(m):
     g = m.graph
     excl = np.ascontiguousarray(np.stack([m.chain_uid, m.res_seq, m.domain_uid, m.bond_uid], 1).astype(np.int32))
@@ -372,14 +396,14 @@ def E_intra(mode, m, data, include_lj_dh=True, table=None, torsV=None, torsS=Non
     return out
 
 
-def E_packed(mode, pos4, meta4, table20, box, nc=False, P=None):
+def E_packed(mode, pos4, meta4, table20, box, nc=False, P=None, repulsive_crowding=False):
     """Reference GPU pair rules on packed arrays: (LJ raw, DH raw, total kcal/mol)."""
     pos4 = np.ascontiguousarray(pos4, np.float32)
     meta4 = np.ascontiguousarray(meta4, np.float32)
     out = np.zeros(3, np.float64)
-    lib().oracle_E_packed(mode, 1 if nc else 0, int(P if P is not None else pos4.shape[0]), pos4.reshape(-1),
-                          meta4.reshape(-1), np.ascontiguousarray(np.asarray(table20, np.float32).reshape(-1)),
-                          float(box), out)
+    lib().oracle_E_packed_rc(mode, 1 if nc else 0, 1 if repulsive_crowding else 0,
+                             int(P if P is not None else pos4.shape[0]), pos4.reshape(-1), meta4.reshape(-1),
+                             np.ascontiguousarray(np.asarray(table20, np.float32).reshape(-1)), float(box), out)
     return out
 
 

@@ -131,6 +131,20 @@ double or_dh_term(int mode, double r, float qi, float qj)
     return (double)qi * (double)qj * exp(-r / (double)OR_XI) / r;
 }
 
+/* Repulsive crowder pair of the reference's REPULSIVE_CROWDING build (off in its
+ * default build, src/definitions.h:18): crowderPairPotential (src/Replica.cpp:416-419)
+ * = powf(6.0f / r, 12.0f) in RT units, applied when r < const_repulsive_cutoff (15 A,
+ * src/definitions.h:38; src/Replica.cpp:443-447 and :464-468), with no Debye-Hueckel
+ * term for the pair.  r includes the +EPS of the callers. */
+double or_crowder_term(int mode, double r)
+{
+    if (!(r < 15.0))
+        return 0.0;
+    if (mode == ORACLE_REF)
+        return (double)powf(6.0f / (float)r, 12.0f);
+    return pow(6.0 / r, 12.0);
+}
+
 /* One residue pair, both terms, in raw units.  r includes the +EPS of the callers. */
 void oracle_pair(int mode, const float *pi, const float *pj, float eps_raw, float qi,
                  float qj, float si, float sj, float box, double *lj, double *dh)
@@ -178,6 +192,34 @@ void oracle_E_inter_matrix(int mode, int nmol, const int *mstart, const int *mco
                     double r = or_dist(mode, xyz + 3 * a, xyz + 3 * b, box) + (double)OR_EPS;
                     LJ += or_lj_term(mode, r, table[aa[a] * ntypes + aa[b]], sig[a], sig[b]);
                     DH += or_dh_term(mode, r, q[a], q[b]);
+                }
+            double e = LJ * OR_RT_TO_KCAL + DH * OR_DHC;
+            out[mI * nmol + mJ] = e;
+            out[mJ * nmol + mI] = e;
+        }
+}
+
+/* The same matrix under repulsive crowding: crowder[m] != 0 marks crowder molecules,
+ * whose pairs (with any molecule) take or_crowder_term and no Debye-Hueckel term
+ * (src/Replica.cpp:434-472). */
+void oracle_E_inter_matrix_rc(int mode, int nmol, const int *mstart, const int *mcount, const int *crowder,
+                              const float *xyz, const int *aa, const float *q, const float *sig,
+                              const float *table, int ntypes, float box, double *out)
+{
+    memset(out, 0, sizeof(double) * nmol * nmol);
+    for (int mI = 0; mI < nmol; mI++)
+        for (int mJ = mI + 1; mJ < nmol; mJ++) {
+            const int crowd = crowder[mI] || crowder[mJ];
+            double LJ = 0.0, DH = 0.0;
+            for (int a = mstart[mI]; a < mstart[mI] + mcount[mI]; a++)
+                for (int b = mstart[mJ]; b < mstart[mJ] + mcount[mJ]; b++) {
+                    double r = or_dist(mode, xyz + 3 * a, xyz + 3 * b, box) + (double)OR_EPS;
+                    if (crowd) {
+                        LJ += or_crowder_term(mode, r);
+                    } else {
+                        LJ += or_lj_term(mode, r, table[aa[a] * ntypes + aa[b]], sig[a], sig[b]);
+                        DH += or_dh_term(mode, r, q[a], q[b]);
+                    }
                 }
             double e = LJ * OR_RT_TO_KCAL + DH * OR_DHC;
             out[mI * nmol + mJ] = e;
@@ -377,8 +419,21 @@ static float frac_part(float w, float *ip)
  * Sums every unordered pair once (the kernel's upper-triangular tiles with halved
  * diagonal tiles).  table20 is the raw 20x20 contact table.  out = {LJ raw, DH raw,
  * total kcal/mol}. */
+void oracle_E_packed_rc(int mode, int nc, int rc, int P, const float *pos4, const float *meta4,
+                        const float *table20, float box, double *out);
+
 void oracle_E_packed(int mode, int nc, int P, const float *pos4, const float *meta4,
                      const float *table20, float box, double *out)
+{
+    oracle_E_packed_rc(mode, nc, 0, P, pos4, meta4, table20, box, out);
+}
+
+/* rc != 0: the REPULSIVE_CROWDING build of E_TiledKernel (src/CudaFunctions.cu:492-498):
+ * a pair that passes the exclusion rules and has a crowder residue (meta w == -1) on
+ * either side adds crowderPotential (6/r)^12 in RT units below 15 A and no
+ * Debye-Hueckel term. */
+void oracle_E_packed_rc(int mode, int nc, int rc, int P, const float *pos4, const float *meta4,
+                        const float *table20, float box, double *out)
 {
     double LJ = 0.0, DH = 0.0;
     for (int y = 0; y < P; y++) {
@@ -404,6 +459,10 @@ void oracle_E_packed(int mode, int nc, int P, const float *pos4, const float *me
             if (excluded)
                 continue;
             double r = or_dist(mode, px, py, box) + (double)OR_EPS;
+            if (rc && (mx[3] == OR_CROWDER || my[3] == OR_CROWDER)) {
+                LJ += or_crowder_term(mode, r);
+                continue;
+            }
             int ax = (int)rintf(mx[0]), ay = (int)rintf(my[0]);
             LJ += or_lj_term(mode, r, table20[ay * 20 + ax], my[2], mx[2]);
             DH += or_dh_term(mode, r, my[1], mx[1]);

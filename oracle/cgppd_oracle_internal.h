@@ -7,6 +7,7 @@
 double or_dist(int mode, const float *a, const float *b, float L);
 double or_lj_term(int mode, double r, float eps_raw, float si, float sj);
 double or_dh_term(int mode, double r, float qi, float qj);
+double or_crowder_term(int mode, double r);
 double or_angle_ref(const float *a, const float *b);
 double or_angle_fp64(const float *pa, const float *pb, const float *pc);
 double or_angle_term(double theta);

@@ -57,6 +57,7 @@ typedef struct {
     float rigid_rotate_p;
     int non_crowders, nc_mode, sample_freq, sample_after;
     float bound_threshold;
+    int rep_crowd; /* REPULSIVE_CROWDING: pairs with a crowder molecule take the crowder term */
 } OracleSystem;
 
 typedef struct {
@@ -142,9 +143,15 @@ static double replica_energy(const OracleSystem *S, int mode, const float *pos, 
     for (int a = 0; a < S->M; ++a)
         for (int b = a + 1; b < S->M; ++b) {
             double lj = 0.0, dh = 0.0;
+            /* REPULSIVE_CROWDING (src/Replica.cpp:434-472): crowder pairs, repulsive only */
+            const int crowd = S->rep_crowd && ((S->mflags[a] | S->mflags[b]) & 2);
             for (int i = S->mstart[a]; i < S->mstart[a] + S->mcount[a]; ++i)
                 for (int j = S->mstart[b]; j < S->mstart[b] + S->mcount[b]; ++j) {
                     double r = or_dist(mode, pos + 3 * i, pos + 3 * j, S->box) + (double)OR_EPS;
+                    if (crowd) {
+                        lj += or_crowder_term(mode, r);
+                        continue;
+                    }
                     lj += or_lj_term(mode, r, S->table[S->aa[i] * S->ntypes + S->aa[j]], S->sig[i], S->sig[j]);
                     dh += or_dh_term(mode, r, S->q[i], S->q[j]);
                 }

@@ -29,7 +29,7 @@ class OracleSystem(ctypes.Structure):
                 ("crank_off", P(c_int)), ("ncrank", P(c_int)), ("crankres", P(c_int)),
                 ("w_cum", c_float * 4), ("w1_cum", c_float * 3), ("rigid_rotate_p", c_float),
                 ("non_crowders", c_int), ("nc_mode", c_int), ("sample_freq", c_int), ("sample_after", c_int),
-                ("bound_threshold", c_float)]
+                ("bound_threshold", c_float), ("rep_crowd", c_int)]
 
 
 class OracleStats(ctypes.Structure):
@@ -82,7 +82,8 @@ class OracleRemc:
 
     def __init__(self, molecules, table, box, temperatures, translate_steps, rotate_steps, move_weights=(1, 1, 1, 1),
                  rigid_rotate_prob=0.5, torsion_V=None, torsion_phase=None, seed=20261203, mode=0,
-                 sample_frequency=0, sample_after=0, bound_threshold=-1.1844, rep_off=0, sim_index=0):
+                 sample_frequency=0, sample_after=0, bound_threshold=-1.1844, rep_off=0, sim_index=0,
+                 repulsive_crowding=False):
         L = _declare()
         self.L = L
         self.keep = []
@@ -208,7 +209,7 @@ class OracleRemc:
             _ptr(offa["local"], c_int), _ptr(cnta["local"], c_int), _ptr(arrs["local"], c_int),
             _ptr(offa["crank"], c_int), _ptr(cnta["crank"], c_int), _ptr(arrs["crank"], c_int),
             (c_float * 4)(*w_cum), (c_float * 3)(*w1_cum), float(rigid_rotate_prob), non_crowders, nc_mode,
-            int(sample_frequency), int(sample_after), float(bound_threshold))
+            int(sample_frequency), int(sample_after), float(bound_threshold), int(bool(repulsive_crowding)))
         # replicas: every slot starts from the same coordinates
         R = len(temperatures)
         self.R = R

@@ -76,3 +76,25 @@ def test_surrogate_batch_must_be_a_multiple_of_128():
     from cgppd_gb300 import surrogate as sg
     with pytest.raises(CgppdError, match="multiple of 128"):
         sg.Surrogate(batch=100)
+
+
+def crowded_engine(order, flexible_crowder=False):
+    e = eng.Engine(table())
+    s = e.add_simulation([300.0, 310.0], [1.0, 1.0], [0.2, 0.2], 100.0, repulsive_crowding=True)
+    for k, crowder in enumerate(order):
+        x = chain(6) + np.float32(20.0 * k)
+        e.add_molecule(s, x, np.arange(6), np.zeros(6), np.full(6, 5.0), crowder=crowder,
+                       all_flexible=flexible_crowder and crowder)
+    return e
+
+
+def test_repulsive_crowding_needs_trailing_crowders():
+    e = crowded_engine([False, True, False])
+    with pytest.raises(CgppdError, match="crowders after every other molecule"):
+        e.finalize(1, 256)
+
+
+def test_repulsive_crowding_needs_rigid_crowders():
+    e = crowded_engine([False, True], flexible_crowder=True)
+    with pytest.raises(CgppdError, match="rigid crowders"):
+        e.finalize(1, 256)

@@ -85,3 +85,15 @@ def test_errors_are_reported(tmp_path):
     bad.write_text("files\np(1,1,1) r(1,0,0,0) a.pdb named\nsegments\nother 1 2 3\n")
     rc, msg = dump(["x", "-f", "bad"], 1 | 2, tmp_path)
     assert rc == 1 and "unknown molecule" in msg
+
+
+def test_repulsive_crowding_key(argdir):
+    # the run-time form of the reference's compile-time REPULSIVE_CROWDING switch:
+    # off unless the argfile sets it
+    rc, p = dump(["x", "tests/argtestfile"], 2 | 8, argdir)
+    assert rc == 0 and p["repulsiveCrowding"] == "0"
+    text = (argdir / "tests" / "argtestfile").read_text()
+    (argdir / "tests" / "crowdfile").write_text("repulsivecrowding 1\n" + text)
+    rc, p = dump(["x", "tests/crowdfile"], 2 | 8, argdir)
+    assert rc == 0, p
+    assert p["repulsiveCrowding"] == "1" and p["nonCrowders"] == "2"
