@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--no-dropin", action="store_true", help="skip the drop-in energy-module leg")
     p.add_argument("--surrogate-workload", default="c4")
     p.add_argument("--surrogate-samples", type=int, default=2_000_000)
     p.add_argument("--surrogate-epochs", type=int, default=8)
@@ -256,6 +257,82 @@ def surrogate_leg(args, torch, flush):
     return out
 
 
+# ------------------------------------------------------------------ drop-in energy module
+
+def dropin_leg(args, torch, flush, wl, peak_tflops):
+    """The reference's energy entry point (CUDA_EonDevice / _async, the drop-in C ABI) on
+    one replica of the workload packed as the reference uploads it: pairs of residues in
+    different molecules (rigid molecules; each molecule its own domain and chain id).
+    Kernel time with events on the call's stream (async form), and the synchronous call
+    (result copied to the host) timed on the host."""
+    import ctypes
+    import cgppd_gb300
+    L = cgppd_gb300.lib()
+    sim = wl.sims[0]
+    mols = sim.molecules
+    N = sum(m.n for m in mols)
+    P = ((N + 31) // 32) * 32
+    pos = np.zeros((P, 4), np.float32)
+    meta = np.zeros((P, 4), np.float32)
+    pos[:, 3] = -2.0   # padding
+    meta[:, 0] = 20.0
+    i0 = 0
+    for k, m in enumerate(mols):
+        sl = slice(i0, i0 + m.n)
+        pos[sl, :3] = m.xyz
+        pos[sl, 3] = k + 1
+        meta[sl, 0] = np.minimum(m.types, 19)
+        meta[sl, 1] = m.charges
+        meta[sl, 2] = m.radii
+        meta[sl, 3] = (k + 1) + (k + 1) / 1024.0
+        i0 += m.n
+    sizes = np.array([m.n for m in mols], np.float64)
+    pairs = float((sizes.sum() ** 2 - (sizes ** 2).sum()) / 2)
+    t20 = np.ascontiguousarray(np.asarray(wl.lj_raw, np.float32)[:20, :20])
+    a = L.cgppd_aminoacids_create()
+    L.cgppd_aminoacids_set_table(a, t20.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    dev = L.LJPotentialDataToDevice(a)
+    L.bindLJTexture(dev)
+    L.CUDA_setBoxDimension(ctypes.c_float(sim.box))
+    dp = torch.from_numpy(pos.reshape(-1)).cuda()
+    dm = torch.from_numpy(meta.reshape(-1)).cuda()
+    rs = P // 32
+    out = torch.zeros(rs * rs, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    args_async = (ctypes.c_void_p(dp.data_ptr()), ctypes.c_void_p(dm.data_ptr()), None, None, None, None,
+                  ctypes.c_void_p(out.data_ptr()), rs, 32, P, 0, ctypes.c_void_p(stream.cuda_stream))
+    reps = 20
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            L.CUDA_EonDevice_async(*args_async)
+        times = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            L.CUDA_EonDevice_async(*args_async)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    cgppd_gb300.check("dropin leg")
+    k_ms = float(np.median(times))
+    res = ctypes.c_double(0.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        L.CUDA_EonDevice(ctypes.c_void_p(dp.data_ptr()), ctypes.c_void_p(dm.data_ptr()), None, None, None, None,
+                         ctypes.byref(res), 32, P, 0)
+    sync_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    cgppd_gb300.check("dropin leg")
+    L.unbindLJTexture()
+    L.cgppd_aminoacids_destroy(a)
+    tflops = pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
+    return {"entry": "CUDA_EonDevice(_async)", "kernel": "k_tile_energy", "workload": wl.name + ", replica 0",
+            "residues": N, "padded": P, "pairs_per_call": pairs, "kernel_ms": k_ms, "sync_call_ms": sync_ms,
+            "pair_evals_per_s": pairs / (k_ms / 1000.0), "achieved_tflops": tflops, "frac": tflops / peak_tflops,
+            "energy_kcal": res.value}
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def gpu_arm(args):
@@ -377,6 +454,9 @@ def gpu_arm(args):
     clocks = clk.summary()
     max_mhz = clocks["sm_max_mhz"] or 2070.0
     peak_tflops = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
+    dropin = None
+    if rank == 0 and world == 1 and not args.no_dropin:
+        dropin = dropin_leg(args, torch, flush, workloads.make("c2"), peak_tflops)
     achieved = k_pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
     traffic = None
     prof = os.path.join(ROOT, "profiles", "dram_traffic.json")
@@ -405,7 +485,7 @@ def gpu_arm(args):
                          "peak_note": "nominal FP32 pipe: SMs x 128 lanes x 2 x max SM clock (no FP32 figure in "
                                       "the measured peaks)"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "surrogate": sur,
+            "surrogate": sur, "dropin": dropin,
         }
         print(json.dumps(out))
     if dist:

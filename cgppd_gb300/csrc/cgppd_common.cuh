@@ -83,10 +83,20 @@ __device__ __forceinline__ float lj_term(float eij, float sigma_ij, float inv_r2
     return u;
 }
 
+// 2^x on the SFU (PTX ex2.approx.ftz.f32, max relative error 2^-22); the Debye-Hueckel
+// argument -r log2(e) / xi reaches the denormal range only beyond r = 873 A, where the
+// term (< 1e-37 kcal/mol) flushes to zero.
+__device__ __forceinline__ float ex2_sfu(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // q_i q_j exp(-r/xi) / r, with exp as ex2 on the SFU.
 __device__ __forceinline__ float dh_term(float qq, float r, float inv_r)
 {
-    return qq * exp2f(r * (-kLog2e / kXi)) * inv_r;
+    return qq * ex2_sfu(r * (-kLog2e / kXi)) * inv_r;
 }
 
 // ------------------------------------------------------------------ Philox4x32-10

@@ -7,9 +7,11 @@
 // crowder).  The pair rules are those of the reference's flexible-linker build.
 //
 // Kernel: one CTA per (y-tile, x-tile) pair of 128-residue tiles on or above the
-// diagonal.  The x tile and the 20x20 table are staged in shared memory, each thread
-// owns one y residue and sweeps the x tile; pair terms are FP32, summed per 32 pairs
-// and folded into float-float accumulators, reduced per CTA in FP64.  The last CTA
+// diagonal.  The x tile is decoded once into shared memory (position and radius; the
+// exclusion keys of its w fields; charge, type and flags) next to the 20x20 table; two
+// threads own each y residue and sweep one half of the x tile each.  Pair terms are
+// FP32, summed per 32 pairs in two alternating partial sums and folded into
+// float-float accumulators, reduced per CTA in FP64.  The last CTA
 // to finish (ticket counter) reduces all CTA partials in a fixed order, so the total
 // is deterministic.  Scratch (partials + ticket + result) is per (device, stream),
 // allocated on first use and reused.
@@ -29,8 +31,9 @@ using namespace cgppd;
 
 namespace {
 
-constexpr int kTile = 128;
-constexpr int kWarps = kTile / 32;
+constexpr int kTile = 128;                 // residues per tile side
+constexpr int kThreads = 2 * kTile;        // two threads per y residue (x-tile halves)
+constexpr int kWarps = kThreads / 32;
 
 __constant__ float c_boxdim;  // CUDA_setBoxDimension, module state per device
 // cgppd_set_repulsive_crowding: the reference's compile-time REPULSIVE_CROWDING
@@ -55,15 +58,20 @@ __device__ __forceinline__ float frac_int(float w, float &ip)
     return w - ip;
 }
 
-template <bool kNC>
-__global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict__ pos, const float4 *__restrict__ meta,
-                                                       int P, int nt, const float *__restrict__ lj_raw,
-                                                       double *__restrict__ partials, unsigned *__restrict__ ticket,
-                                                       unsigned *__restrict__ flags, double *__restrict__ result,
-                                                       float *__restrict__ async_out, int async_count, int rc)
+// kNC: non-crowder pairs of different molecules only (E_TiledKernelNC).  kRC: the
+// REPULSIVE_CROWDING form of the crowder pairs.
+template <bool kNC, bool kRC>
+__global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restrict__ pos, const float4 *__restrict__ meta,
+                                                          int P, int nt, const float *__restrict__ lj_raw,
+                                                          double *__restrict__ partials, unsigned *__restrict__ ticket,
+                                                          unsigned *__restrict__ flags, double *__restrict__ result,
+                                                          float *__restrict__ async_out, int async_count)
 {
-    __shared__ float4 s_pos[kTile];
-    __shared__ float4 s_meta[kTile];
+    // x tile, decoded once per CTA: position and vdW radius; exclusion keys (rigid
+    // domain, bond fraction, chain fraction, molecule id); charge, type, flags
+    __shared__ float4 s_px[kTile];
+    __shared__ float4 s_xk[kTile];
+    __shared__ float4 s_xm[kTile];
     __shared__ float s_eij[400];
     __shared__ double s_red[2][kWarps];
     __shared__ bool s_last;
@@ -76,76 +84,104 @@ __global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict_
     }
     const int tx = ty + rem;
     const int t = threadIdx.x;
+    const int yl = t & (kTile - 1), half = t / kTile;  // y residue, half of the x tile
 
-    for (int k = t; k < 400; k += kTile)
+    for (int k = t; k < 400; k += kThreads)
         s_eij[k] = kLambda * (lj_raw[k] - kE0);  // Eij in RT units, as the kernel forms it
-    const float4 pad = make_float4(0.f, 0.f, 0.f, kPadder);
-    const float4 padm = make_float4(20.f, 0.f, 0.f, 0.f);
+    // residue types are checked once per residue (0..19; padding is excluded anyway):
+    // the pair loop then indexes the table without a bounds test
+    unsigned bad = 0;
     const int x0 = tx * kTile;
-    s_pos[t] = (x0 + t < P) ? pos[x0 + t] : pad;
-    s_meta[t] = (x0 + t < P) ? meta[x0 + t] : padm;
-    const int y = ty * kTile + t;
-    const float4 py = (y < P) ? pos[y] : pad;
-    const float4 my = (y < P) ? meta[y] : padm;
+    if (t < kTile) {
+        const float4 px = (x0 + t < P) ? pos[x0 + t] : make_float4(0.f, 0.f, 0.f, kPadder);
+        const float4 mx = (x0 + t < P) ? meta[x0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float xdom, xmol;
+        const float xbond = frac_int(px.w, xdom);
+        const float xchain = frac_int(mx.w, xmol);
+        const bool pad = px.w == kPadder;
+        const bool crowd = mx.w == kCrowder;
+        int xt = __float2int_rn(mx.x);
+        if ((unsigned)xt >= 20u) {
+            // crowders read no table entry where they are excluded (kNC) or repulsive
+            // only (kRC; the reference then gives them the type -1)
+            bad |= (pad || (crowd && (kNC || kRC))) ? 0u : 1u;
+            xt = 0;
+        }
+        const int xflags = (pad ? 1 : 0) | (crowd ? 2 : 0);
+        s_px[t] = make_float4(px.x, px.y, px.z, mx.z);
+        s_xk[t] = make_float4(xdom, xbond, xchain, xmol);
+        s_xm[t] = make_float4(mx.y, __int_as_float(xt), __int_as_float(xflags), 0.f);
+    }
+    const int y = ty * kTile + yl;
+    const float4 py = (y < P) ? pos[y] : make_float4(0.f, 0.f, 0.f, kPadder);
+    const float4 my = (y < P) ? meta[y] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
 
     FF lj{0.f, 0.f}, dh{0.f, 0.f};
-    unsigned bad = 0;
-    const bool active = (py.w > kPadder) && (!kNC || my.w != kCrowder);
+    const bool ycrowd = my.w == kCrowder;
+    const bool active = (py.w > kPadder) && (!kNC || !ycrowd);
     if (active) {
         const float L = c_boxdim;
         const float invL = (L != 0.0f) ? 1.0f / L : 0.0f;
         float ydom, ymol;
         const float ybond = frac_int(py.w, ydom);
         const float ychain = frac_int(my.w, ymol);
+        const bool ydom_nz = ydom != 0.f, ybond_nz = ybond != 0.f;
         const bool diag = (tx == ty);
-        const bool ycrowd = rc && (my.w == kCrowder);
-        for (int jb = 0; jb < kTile; jb += 32) {
-            float lj_t = 0.f, dh_t = 0.f;
+        // the chain rule (|x - y| < 4) can only hold on and next to the diagonal
+        const bool near = (tx - ty) <= 1;
+        int yt = __float2int_rn(my.x);
+        if ((unsigned)yt >= 20u) {
+            bad |= (kRC && ycrowd) ? 0u : 1u;
+            yt = 0;
+        }
+        const float *erow = s_eij + 20 * yt;
+        const float yq = my.y, ys = my.z;
+        const int jb0 = half * (kTile / 2);
+        for (int jb = jb0; jb < jb0 + kTile / 2; jb += 32) {
+            float l0 = 0.f, l1 = 0.f, d0 = 0.f, d1 = 0.f;
+            // branch-free: every pair is evaluated and the excluded ones (padding, the
+            // pair itself on the diagonal: possibly inf / NaN) are selected away
 #pragma unroll 4
             for (int jj = 0; jj < 32; ++jj) {
                 const int j = jb + jj;
-                const float4 px = s_pos[j];
-                const float4 mx = s_meta[j];
-                bool excl = (px.w == kPadder) || (diag && j <= t);
-                if (kNC) {
-                    excl = excl || (mx.w == kCrowder) || (truncf(mx.w) == ymol);
-                } else {
-                    float xdom, xmol;
-                    const float xbond = frac_int(px.w, xdom);
-                    const float xchain = frac_int(mx.w, xmol);
-                    excl = excl || (xdom != 0.f && xdom == ydom) || (xbond != 0.f && xbond == ybond) ||
-                           (xchain == ychain && fabsf((float)(x0 + j) - (float)y) < 4.0f);
+                const float4 xk = s_xk[j];
+                const float4 xm = s_xm[j];
+                const float4 px = s_px[j];
+                const int xflags = __float_as_int(xm.z);
+                bool excl = (xflags & 1) || (diag && j <= yl);
+                if (kNC)
+                    excl = excl || (xflags & 2) || xk.w == ymol;
+                else
+                    excl = excl || (ydom_nz && xk.x == ydom) || (ybond_nz && xk.y == ybond) ||
+                           (near && xk.z == ychain && abs(x0 + j - y) < 4);
+                const float dx = min_image(py.x - px.x, L, invL);
+                const float dyy = min_image(py.y - px.y, L, invL);
+                const float dz = min_image(py.z - px.z, L, invL);
+                const float r2 = fmaf(dx, dx, fmaf(dyy, dyy, dz * dz));
+                const float inv_r = rsqrt_refined(r2);
+                const float r = r2 * inv_r;
+                float lt = lj_term(erow[__float_as_int(xm.y)], (ys + px.w) * 0.5f, inv_r * inv_r);
+                float dt = dh_term(yq * xm.x, r, inv_r);
+                if (kRC && (ycrowd || (xflags & 2))) {
+                    // REPULSIVE_CROWDING (src/CudaFunctions.cu:335-338, :492-498):
+                    // (6/r)^12 in RT units below 15 A, no Debye-Hueckel term
+                    const float sc = 6.0f * inv_r, s2 = sc * sc, s6 = s2 * s2 * s2;
+                    lt = (r < kRepulsiveCutoff) ? s6 * s6 : 0.f;
+                    dt = 0.f;
                 }
-                if (!excl) {
-                    const float dx = min_image(py.x - px.x, L, invL);
-                    const float dy = min_image(py.y - px.y, L, invL);
-                    const float dz = min_image(py.z - px.z, L, invL);
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float inv_r = rsqrt_refined(r2);
-                    const float r = r2 * inv_r;
-                    if (ycrowd || (rc && mx.w == kCrowder)) {
-                        // REPULSIVE_CROWDING (src/CudaFunctions.cu:335-338, :492-498):
-                        // (6/r)^12 in RT units below 15 A, no Debye-Hueckel term
-                        if (r < kRepulsiveCutoff) {
-                            const float sc = 6.0f * inv_r, s2 = sc * sc, s6 = s2 * s2 * s2;
-                            lj_t += s6 * s6;
-                        }
-                    } else {
-                        int idx = __float2int_rn(20.0f * my.x + mx.x);
-                        if ((unsigned)idx >= 400u) {
-                            bad = 1u;
-                            idx = 0;
-                        }
-                        const float eij = s_eij[idx];
-                        const float sig = (my.z + mx.z) * 0.5f;
-                        lj_t += lj_term(eij, sig, inv_r * inv_r);
-                        dh_t += dh_term(my.y * mx.y, r, inv_r);
-                    }
+                lt = excl ? 0.f : lt;
+                dt = excl ? 0.f : dt;
+                if (jj & 1) {
+                    l1 += lt;
+                    d1 += dt;
+                } else {
+                    l0 += lt;
+                    d0 += dt;
                 }
             }
-            ff_add(lj, lj_t);
-            ff_add(dh, dh_t);
+            ff_add(lj, l0 + l1);
+            ff_add(dh, d0 + d1);
         }
     }
 
@@ -183,7 +219,7 @@ __global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict_
     // Last CTA: ordered reduction of every CTA's partials.
     __threadfence();
     double a = 0.0, b = 0.0;
-    for (int k = t; k < (int)gridDim.x; k += kTile) {
+    for (int k = t; k < (int)gridDim.x; k += kThreads) {
         a += __ldcg(&partials[2 * k]);
         b += __ldcg(&partials[2 * k + 1]);
     }
@@ -213,7 +249,7 @@ __global__ void __launch_bounds__(kTile) k_tile_energy(const float4 *__restrict_
         *ticket = 0u;
     }
     if (async_out != nullptr)
-        for (int k = 1 + t; k < async_count; k += kTile)
+        for (int k = 1 + t; k < async_count; k += kThreads)
             async_out[k] = 0.0f;
 }
 
@@ -259,13 +295,17 @@ int launch_energy(bool nc, const float4 *pos, const float4 *meta, int P, const f
 {
     const int nt = (P + kTile - 1) / kTile;
     const int blocks = nt * (nt + 1) / 2;
-    const int rc = g_repulsive_crowding.load();
+    // crowders take no part in the non-crowder sum, so its form has no crowder variant
+    const bool rc = g_repulsive_crowding.load() != 0;
     if (nc)
-        k_tile_energy<true><<<blocks, kTile, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket, s->flags,
-                                                           s->result, async_out, async_count, rc);
+        k_tile_energy<true, false><<<blocks, kThreads, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket,
+                                                                    s->flags, s->result, async_out, async_count);
+    else if (rc)
+        k_tile_energy<false, true><<<blocks, kThreads, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket,
+                                                                    s->flags, s->result, async_out, async_count);
     else
-        k_tile_energy<false><<<blocks, kTile, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket, s->flags,
-                                                            s->result, async_out, async_count, rc);
+        k_tile_energy<false, false><<<blocks, kThreads, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket,
+                                                                     s->flags, s->result, async_out, async_count);
     return cgppd_check(cudaGetLastError(), "energy kernel launch");
 }
 

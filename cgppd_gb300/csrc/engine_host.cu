@@ -676,7 +676,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
             // (a difference swamped by noise falls back to the plain per-step time)
             const float us = (t2 > t1) ? 1000.f * (t2 - t1) / n : 1000.f * t2 / (2 * n);
             e->tuning.push_back({C, T, us});
-            if (us < best * 0.97f) {  // prefer the smaller shape unless clearly faster
+            if (us < best * 0.995f) {  // ties (within timing noise) keep the smaller shape
                 best = us;
                 bc = C;
                 bt = T;

@@ -329,14 +329,6 @@ __device__ __forceinline__ float3 normalized(float x, float y, float z)
     return make_float3(x, y, z);
 }
 
-// 2^x on the SFU (PTX ex2.approx.ftz.f32, max relative error 2^-22); the Debye-Hueckel
-// argument -r log2(e) / xi stays far from the denormal range for r > 0.
-__device__ __forceinline__ float ex2_sfu(float x)
-{
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
 
 // Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with
 // (q*sqrt(DHF), type) in qa/qb.  `table` holds -4 Eij (kcal/mol): the LJ term is
