@@ -525,110 +525,170 @@ __device__ __forceinline__ T ld_state(const T *p)
     return __ldcg(p);
 }
 
-template <bool RES>
-__device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols, const float4 *CEN,
-                            const float4 *P, float tstep, float rstep, const float4 rsc, const uint32_t *w,
-                            MoveDesc &mv)
+// The part of a move decision that depends on the draws alone (src/Molecule.cpp:146-504:
+// the molecule, the move type, the direction and its rotation, the flex residue and
+// branch, the local residue and the crankshaft flip), taken one step ahead by a warp
+// that would otherwise wait; finish_move adds the part that reads the state.
+struct MovePre {
+    int m, type, kind, ri, br_off, br_cnt, null_move, flip;
+    float ux, uy, uz;
+    float R[9];
+    uint32_t w_metro, w_stage1;
+};
+
+__device__ void predecide_move(const Lists &a, const DevSim &S, const DevMol *mols, const float4 rsc,
+                               const uint32_t *w, MovePre &pre)
 {
     const int M = S.M;
-    mv.m = pickw(w[0], M);
-    const DevMol mol = mols[mv.m];
-    mv.start = mol.start;
-    mv.n = mol.count;
-    mv.flexible = (mol.flags & kMolFlexible) != 0;
-    mv.nintra = mol.nintra;
-    mv.null_move = 0;
-    mv.wrapped = 0;
-    const float box = S.box;
-    const float4 c = ld_state<RES>(&CEN[mv.m]);
-    mv.cx = c.x, mv.cy = c.y, mv.cz = c.z;
-    mv.wcx = c.x, mv.wcy = c.y, mv.wcz = c.z;
-    if (mv.flexible) {
+    const int m = pickw(w[0], M);
+    const DevMol &mol = mols[m];
+    pre.m = m;
+    pre.kind = 0, pre.ri = 0, pre.br_off = 0, pre.br_cnt = 0, pre.null_move = 0, pre.flip = 0;
+    int type;
+    if (mol.flags & kMolFlexible) {
         int k = 0;
         if (M > 1) {
             while (k < 3 && (unsigned long long)w[1] >= S.thr4[k])
                 ++k;
-            mv.type = k;
+            type = k;
         } else {
             while (k < 2 && (unsigned long long)w[1] >= S.thr3[k])
                 ++k;
-            mv.type = 1 + k;
+            type = 1 + k;
         }
     } else {
-        mv.type = ((unsigned long long)w[1] < S.thr_rot) ? kRotate : kTranslate;  // gsl_ran_bernoulli
+        type = ((unsigned long long)w[1] < S.thr_rot) ? kRotate : kTranslate;  // gsl_ran_bernoulli
     }
+    pre.type = type;
     const float dx = centred(w[2], false), dy = centred(w[3], true), dz = centred(w[4], false);
-    const float4 *Pm = P + mv.start;
-
-    switch (mv.type) {
+    switch (type) {
     case kTranslate: {
         // Molecule::translate(rng, step) (src/Molecule.cpp:146-159, :262-266)
         const float3 u = normalized(dx, dy, dz);
-        mv.vx = u.x * tstep, mv.vy = u.y * tstep, mv.vz = u.z * tstep;
-        mv.wcx = wrapf(c.x + mv.vx, box);
-        mv.wcy = wrapf(c.y + mv.vy, box);
-        mv.wcz = wrapf(c.z + mv.vz, box);
+        pre.ux = u.x, pre.uy = u.y, pre.uz = u.z;
         break;
     }
     case kRotate: {
         // Molecule::rotate(rng, step) -> setRotation (src/Molecule.cpp:193-208, :255-260)
         const float3 u = normalized(dx, dy, dz);
-        axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, true, mv.R);
+        axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, true, pre.R);
         break;
     }
     case kFlex: {
         // Molecule::flex(rng, step) (src/Molecule.cpp:331-413)
         if (mol.nflex == 0) {
-            mv.null_move = 1;
+            pre.null_move = 1;
             break;
         }
         const float3 u = normalized(dx, dy, dz);
-        axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, false, mv.R);
+        axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, false, pre.R);
         const int4 fr = a.flexres[mol.flex_off + pickw(w[5], mol.nflex) - a.base[kLFlex]];
         if (fr.y <= 0) {
-            mv.null_move = 1;
+            pre.null_move = 1;
             break;
         }
         const int4 op = a.flexopt[fr.z + pickw(w[6], fr.y) - a.base[kLFopt]];
-        mv.ri = fr.x;
-        mv.br_off = op.y;
-        mv.br_cnt = op.z;
-        const float4 p = ld_state<RES>(&Pm[fr.x]);
-        mv.px = p.x, mv.py = p.y, mv.pz = p.z;
+        pre.ri = fr.x;
+        pre.br_off = op.y;
+        pre.br_cnt = op.z;
         break;
     }
     case kLocal: {
         // Molecule::make_local_moves (src/Molecule.cpp:415-448): Bernoulli(0.5) picks a
         // crankshaft (1) or a local translation (0) of one residue.
-        mv.kind = (w[5] < 2147483648u) ? 1 : 0;
-        float vx, vy, vz;
-        if (mv.kind == 0) {
+        pre.kind = (w[5] < 2147483648u) ? 1 : 0;
+        if (pre.kind == 0) {
             if (mol.nlocal == 0) {
-                mv.null_move = 1;
+                pre.null_move = 1;
                 break;
             }
-            mv.ri = a.localres[mol.local_off + pickw(w[6], mol.nlocal) - a.base[kLLocal]];
+            pre.ri = a.localres[mol.local_off + pickw(w[6], mol.nlocal) - a.base[kLLocal]];
             const float3 u = normalized(dx, dy, dz);
-            const float s = (float)((double)0.1f * (double)tstep);
-            vx = u.x * s, vy = u.y * s, vz = u.z * s;
+            pre.ux = u.x, pre.uy = u.y, pre.uz = u.z;
         } else {
             if (mol.ncrank == 0) {
-                mv.null_move = 1;
+                pre.null_move = 1;
                 break;
             }
             const int ri = a.crankres[mol.crank_off + pickw(w[6], mol.ncrank) - a.base[kLCrank]];
-            if (ri < 1 || ri + 1 >= mv.n) {  // needs both backbone neighbours in the array
-                mv.null_move = 1;
+            if (ri < 1 || ri + 1 >= mol.count) {  // needs both backbone neighbours in the array
+                pre.null_move = 1;
                 break;
             }
-            mv.ri = ri;
-            const bool flip = w[7] < 2147483648u;
+            pre.ri = ri;
+            pre.flip = w[7] < 2147483648u;
+        }
+        break;
+    }
+    }
+    pre.w_metro = w[8];
+    pre.w_stage1 = w[9];
+}
+
+// The move of this step from its draw-only part and the current state: the centre,
+// the translation and its wrap, the flex pivot, the crankshaft rotation.
+template <bool RES>
+__device__ void finish_move(const DevSim &S, const DevMol *mols, const float4 *CEN, const float4 *P, float tstep,
+                            const float4 rsc, const MovePre &pre, MoveDesc &mv)
+{
+    const int m = pre.m;
+    const DevMol &mol = mols[m];
+    mv.m = m;
+    mv.start = mol.start;
+    mv.n = mol.count;
+    mv.flexible = (mol.flags & kMolFlexible) != 0;
+    mv.nintra = mol.nintra;
+    mv.type = pre.type;
+    mv.kind = pre.kind;
+    mv.ri = pre.ri;
+    mv.br_off = pre.br_off;
+    mv.br_cnt = pre.br_cnt;
+    mv.null_move = pre.null_move;
+    mv.wrapped = 0;
+    mv.w_metro = pre.w_metro;
+    mv.w_stage1 = pre.w_stage1;
+    const float box = S.box;
+    const float4 c = ld_state<RES>(&CEN[m]);
+    mv.cx = c.x, mv.cy = c.y, mv.cz = c.z;
+    mv.wcx = c.x, mv.wcy = c.y, mv.wcz = c.z;
+    const float4 *Pm = P + mv.start;
+    switch (pre.type) {
+    case kTranslate:
+        mv.vx = pre.ux * tstep, mv.vy = pre.uy * tstep, mv.vz = pre.uz * tstep;
+        mv.wcx = wrapf(c.x + mv.vx, box);
+        mv.wcy = wrapf(c.y + mv.vy, box);
+        mv.wcz = wrapf(c.z + mv.vz, box);
+        break;
+    case kRotate:
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            mv.R[k] = pre.R[k];
+        break;
+    case kFlex: {
+        if (pre.null_move)
+            break;
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            mv.R[k] = pre.R[k];
+        const float4 p = ld_state<RES>(&Pm[pre.ri]);
+        mv.px = p.x, mv.py = p.y, mv.pz = p.z;
+        break;
+    }
+    case kLocal: {
+        if (pre.null_move)
+            break;
+        float vx, vy, vz;
+        if (pre.kind == 0) {
+            const float s = (float)((double)0.1f * (double)tstep);
+            vx = pre.ux * s, vy = pre.uy * s, vz = pre.uz * s;
+        } else {
+            const int ri = pre.ri;
             const float4 pm = ld_state<RES>(&Pm[ri - 1]);
             const float4 p0 = ld_state<RES>(&Pm[ri]);
             const float4 pp = ld_state<RES>(&Pm[ri + 1]);
             const float3 ax = normalized(pp.x - pm.x, pp.y - pm.y, pp.z - pm.z);
             float Rm[9];
-            axis_angle_matrix_sc(flip ? rsc.z : rsc.x, flip ? rsc.w : rsc.y, ax.x, ax.y, ax.z, true, Rm);
+            axis_angle_matrix_sc(pre.flip ? rsc.z : rsc.x, pre.flip ? rsc.w : rsc.y, ax.x, ax.y, ax.z, true, Rm);
             const float3 rr = rot_apply(Rm, p0.x - pm.x, p0.y - pm.y, p0.z - pm.z);
             vx = (rr.x + pm.x) - p0.x;
             vy = (rr.y + pm.y) - p0.y;
@@ -647,8 +707,6 @@ __device__ void decide_move(const Lists &a, const DevSim &S, const DevMol *mols,
         break;
     }
     }
-    mv.w_metro = w[8];
-    mv.w_stage1 = w[9];
 }
 
 // ------------------------------------------------------------------ surrogate screening
@@ -886,6 +944,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ MoveDesc mv;
+    __shared__ MovePre s_pre;      // the next step's draw-only decision
     __shared__ FF s_red[kMaxWarps];
     __shared__ float s_fred[3 * kMaxWarps];
     // running total, old/new row of the moved molecule and its internal energy, all as
@@ -1102,15 +1161,35 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         }
     }
 
-    for (int step = 0; step < nsteps; ++step) {
-        const unsigned long long mcstep = step0 + (unsigned long long)step;
-        // ---- the move decision (thread 0) from the words drawn one step ahead
-        if (t == 0) {
+    // the first step's draw-only decision (later ones are taken a step ahead by the
+    // last warp while warp 0 runs the Metropolis test)
+    if (t == 0) {
+        uint32_t w[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k)
+            w[k] = s_w[k];
+        predecide_move(Ls, S, s_mols, rsc, w, s_pre);
+    }
+    __syncthreads();
+    // the next step's words and draw-only decision, by the last warp
+    auto draw_ahead = [&](unsigned long long next) {
+        draw(next);
+        __syncwarp();
+        if (lane == 0) {
             uint32_t w[12];
 #pragma unroll
             for (int k = 0; k < 12; ++k)
                 w[k] = s_w[k];
-            decide_move<RES>(Ls, S, s_mols, CEN, P, tstep, rstep, rsc, w, mv);
+            predecide_move(Ls, S, s_mols, rsc, w, s_pre);
+        }
+    };
+
+    for (int step = 0; step < nsteps; ++step) {
+        const unsigned long long mcstep = step0 + (unsigned long long)step;
+        // ---- the move decision (thread 0): the state-dependent part of the decision
+        // taken a step ahead
+        if (t == 0) {
+            finish_move<RES>(S, s_mols, CEN, P, tstep, rsc, s_pre, mv);
             if (RES)
                 s_old_row = ROWSUMf[mv.m];
         }
@@ -1553,6 +1632,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 if (nullm)
                     errbits |= 1u;
             }
+        } else if (warp == NW - 1) {
+            draw_ahead(mcstep + 1);  // (thread 0 consumed this step's decision before the first barrier)
         }
         __syncthreads();
 
@@ -1604,10 +1685,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
         }
         }  // !skip
-        // the next step's words, by the last warp (thread 0 read this step's before the
-        // step's first barrier; the end-of-step barrier publishes these)
-        if (warp == NW - 1)
-            draw(mcstep + 1);
+        // a step the surrogate rejected skipped the Metropolis slot: the next step's words
+        // and decision here (the end-of-step barrier publishes them)
+        if (skip && warp == NW - 1)
+            draw_ahead(mcstep + 1);
         // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
         const int freq = S.sample_freq;
         if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&
