@@ -245,6 +245,25 @@ __device__ FF block_sum_ff_ff(FF v, FF *red)
     return s;
 }
 
+// Block-wide FF sum in a fixed order, complete in every lane of warp 0 (a butterfly over
+// the warp sums; the other warps' return value is unspecified).
+__device__ FF block_sum_ff_warp0(FF v, FF *red)
+{
+    const int t = threadIdx.x, nw = blockDim.x >> 5, lane = t & 31;
+    v = ff_warp_sum(v);
+    __syncthreads();
+    if (lane == 0)
+        red[t >> 5] = v;
+    __syncthreads();
+    FF s{0.f, 0.f};
+    if (t < 32) {
+        if (lane < nw)
+            s = red[lane];
+        s = ff_warp_sum(s);
+    }
+    return s;
+}
+
 // Block-wide FF sum in a fixed order, returned as double in every thread.
 __device__ double block_sum_ff(FF v, FF *red)
 {
@@ -1516,20 +1535,19 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int M1 = a.max_m + 1;
         FF *rcv = reinterpret_cast<FF *>(smem + Ly.rcv) + (step & 1) * C * M1;
         for (int b = warp; b < M; b += NW) {
+            if (b == m)  // the mover's own row is not read
+                continue;
             FF acc{0.f, 0.f};
-            if (b != m) {
-                const DevMol &mb = s_mols[b];
-                const int ob0 = (mb.start < start) ? mb.start : mb.start - n;
-                const int lo = max(ob0, o0), hi = min(ob0 + mb.count, o1);
-                for (int o = lo + lane; o < hi; o += 32) {
-                    const float2 e = s_ej[o - o0];
-                    ff_add_ff(acc, FF{e.x, e.y});
-                }
-                acc = ff_warp_sum(acc);
+            const DevMol &mb = s_mols[b];
+            const int ob0 = (mb.start < start) ? mb.start : mb.start - n;
+            const int lo = max(ob0, o0), hi = min(ob0 + mb.count, o1);
+            for (int o = lo + lane; o < hi; o += 32) {
+                const float2 e = s_ej[o - o0];
+                ff_add_ff(acc, FF{e.x, e.y});
             }
+            acc = ff_warp_sum(acc);
             // lane 0's value for every receiver (lanes may differ in the low word)
-            const FF v{__shfl_sync(0xffffffffu, (b != m) ? acc.hi : 0.f, 0),
-                       __shfl_sync(0xffffffffu, (b != m) ? acc.lo : 0.f, 0)};
+            const FF v{__shfl_sync(0xffffffffu, acc.hi, 0), __shfl_sync(0xffffffffu, acc.lo, 0)};
             if (C > 1) {
                 if (lane < C)
                     cg::this_cluster().map_shared_rank(rcv, lane)[rank * M1 + b] = v;
@@ -1538,7 +1556,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
         }
         if (flexmol) {
-            const FF v = block_sum_ff_ff(iacc, s_red);
+            const FF v = block_sum_ff_warp0(iacc, s_red);
             if (C > 1) {
                 if (t < C)
                     cg::this_cluster().map_shared_rank(rcv, t)[rank * M1 + a.max_m] = v;
@@ -1558,6 +1576,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         if (warp == 0) {
             FF v{0.f, 0.f};
             for (int b = lane; b < M; b += 32) {
+                if (b == m)
+                    continue;
                 FF rb{0.f, 0.f};
                 if (C > 1) {
                     for (int k = 0; k < C; ++k)
@@ -1566,21 +1586,30 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 } else {
                     rb = s_rowp[b];
                 }
-                if (b != m)
-                    ff_add_ff(v, rb);
+                ff_add_ff(v, rb);
             }
-            v = ff_warp_sum(v);
-            if (lane == 0) {
-                FF intra_new{0.f, 0.f};
-                if (flexmol) {
-                    if (C > 1)
-                        for (int k = 0; k < C; ++k)
-                            ff_add_ff(intra_new, rcv[k * M1 + a.max_m]);
-                    else
-                        intra_new = s_intrap;
-                    if (incr)  // the partials are the change: add the molecule's current value
-                        ff_add_ff(intra_new, INTRAf[m]);
+            if (M > 1)
+                v = ff_warp_sum(v);
+            // the internal energy's partials of the C ranks: lane k holds rank k's, summed
+            // in a fixed tree towards lane 0
+            FF intra_new{0.f, 0.f};
+            if (flexmol) {
+                if (C > 1) {
+                    if (lane < C)
+                        intra_new = rcv[lane * M1 + a.max_m];
+                    for (int d = 1; d < C; d <<= 1) {
+                        const FF w{__shfl_down_sync(0xffffffffu, intra_new.hi, d),
+                                   __shfl_down_sync(0xffffffffu, intra_new.lo, d)};
+                        if (lane + d < C)
+                            ff_add_ff(intra_new, w);
+                    }
+                } else {
+                    intra_new = s_intrap;
                 }
+            }
+            if (lane == 0) {
+                if (flexmol && incr)  // the partials are the change: add the molecule's current value
+                    ff_add_ff(intra_new, INTRAf[m]);
                 s_intra_new = intra_new;
                 FF new_row = v;
                 ff_add_ff(new_row, intra_new);
