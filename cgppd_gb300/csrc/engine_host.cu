@@ -145,7 +145,7 @@ struct cgppd_engine {
 
     // device buffers
     DevBuf<DevSim> d_sims;
-    DevBuf<int> d_rep_sim;
+    DevBuf<int> d_rep_sim, d_rep_order;
     DevBuf<DevMol> d_mols;
     DevBuf<float4> d_rstat;
     DevBuf<int4> d_rexcl;
@@ -188,6 +188,7 @@ struct cgppd_engine {
         EngineArgs a{};
         a.sims = d_sims.ptr;
         a.rep_sim = d_rep_sim.ptr;
+        a.rep_order = d_rep_order.ptr;
         a.mols = d_mols.ptr;
         a.rstat = d_rstat.ptr;
         a.rexcl = d_rexcl.ptr;
@@ -523,10 +524,29 @@ int cgppd_engine::build()
     }
     total_replicas = rep_off;
     std::vector<int> sim_state(4 * sims.size(), 0);
+    // k_mc's clusters run each replica to the end of the block and the next waits for
+    // a free SM: the replicas with the most pair work per step go first (longest
+    // processing time first), so the launch does not end on a few long replicas
+    std::vector<double> sim_work(sims.size(), 0.0);
+    for (size_t s = 0; s < sims.size(); ++s) {
+        const HostSim &hs = sims[s];
+        double N = 0.0, w = 0.0;
+        for (auto &m : hs.mols)
+            N += m.n;
+        for (auto &m : hs.mols)
+            w += (double)m.n * (N - m.n);
+        sim_work[s] = w / (double)hs.mols.size();
+    }
+    std::vector<int> rep_order(total_replicas);
+    for (int g = 0; g < total_replicas; ++g)
+        rep_order[g] = g;
+    std::stable_sort(rep_order.begin(), rep_order.end(),
+                     [&](int x, int y) { return sim_work[rep_sim[x]] > sim_work[rep_sim[y]]; });
 
     int rc = 0;
     rc |= d_sims.upload(h_sims);
     rc |= d_rep_sim.upload(rep_sim);
+    rc |= d_rep_order.upload(rep_order);
     rc |= d_mols.upload(h_mols);
     rc |= d_rstat.upload(rstat);
     rc |= d_rexcl.upload(rexcl);

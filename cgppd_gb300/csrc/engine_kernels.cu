@@ -984,7 +984,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     int rank = 0;
     if (C > 1)
         rank = (int)cg::this_cluster().block_rank();
-    const int g = blockIdx.x / C;
+    const int g = a.rep_order[blockIdx.x / C];
     const int s = a.rep_sim[g];
     if (t == 0) {
         S = a.sims[s];

@@ -93,6 +93,7 @@ struct ReplicaStats {
 struct EngineArgs {
     const DevSim *sims;
     const int *rep_sim;          // global replica -> simulation
+    const int *rep_order;        // launch order of k_mc: cluster index -> global replica
     const DevMol *mols;
     const float4 *rstat;
     const int4 *rexcl;
