@@ -13,9 +13,13 @@
  *   - Replica::E()                 src/Replica.cpp:421-500  (inter-molecule pairs)
  *   - Replica::E(a,b)              src/Replica.cpp:502-528
  *   - Molecule::E(bool)            src/Molecule.cpp:636-699 (flexible intra + bonded)
+ *   - crowderPairPotential and the REPULSIVE_CROWDING branches of Replica::E()
+ *                                  src/Replica.cpp:416-472 (off in the reference's
+ *                                  default build; selected per call here)
  * and, on the packed float4 layout, the pair rules of the reference GPU kernels
  *   - E_TiledKernel   src/CudaFunctions.cu:346-607 (flexible-linker build)
  *   - E_TiledKernelNC src/CudaFunctions.cu:757-961
+ *   - the REPULSIVE_CROWDING branch of E_TiledKernel, src/CudaFunctions.cu:492-498
  *
  * Every energy function takes `mode`:
  *   ORACLE_REF  (0): the reference's own mixed precision -- float coordinates and
