@@ -77,7 +77,7 @@ int cgppd_engine_surrogate_compatible(struct cgppd_engine *e, int sim);
  * the engine or be detached first.  `rmse_threshold` (kcal/mol): a simulation falls
  * back to the plain test once the RMS of (exact - surrogate) energy changes over an
  * exchange block's second-stage evaluations with |exact change| <= `error_window`
- * exceeds it (judged after every block with at least `min_evals` such evaluations).
+ * exceeds it (checked after every block with at least `min_evals` such evaluations).
  * Delayed acceptance needs 4 or 8 CTAs per replica; the launch shape is re-chosen. */
 int cgppd_engine_set_surrogate(struct cgppd_engine *e, cgppd_surrogate *s, float rmse_threshold,
                                float error_window, int min_evals);
