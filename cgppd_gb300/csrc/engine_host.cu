@@ -1332,6 +1332,17 @@ unsigned cgppd_engine_error_bits(cgppd_engine *e)
     return o;
 }
 
+int cgppd_engine_replica_error_bits(cgppd_engine *e, int sim, unsigned *out)
+{
+    if (!e->finalized || sim < 0 || sim >= (int)e->h_sims.size() || !out)
+        return cgppd_fail("cgppd_engine_replica_error_bits: bad index");
+    const DevSim &S = e->h_sims[sim];
+    if (cgppd_check(cudaDeviceSynchronize(), "replica error bits") != 0)
+        return -1;
+    return cgppd_check(cudaMemcpy(out, e->d_errflags.ptr + S.rep_off, sizeof(unsigned) * S.R, cudaMemcpyDeviceToHost),
+                       "replica error bits");
+}
+
 int cgppd_engine_last_launches(const cgppd_engine *e) { return e->last_launches; }
 
 int cgppd_engine_set_resident(cgppd_engine *e, int allow)

@@ -1620,7 +1620,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 if (DA && screened)  // stage 2: exact change less the surrogate's
                     delta = (float)(ff_value(dEf) - s_ds);
                 int acc = 0;
-                if (delta < 0.0f) {
+                if (!isfinite(dEf.hi) || !isfinite(delta)) {
+                    // a non-finite energy change (non-finite coordinates): rejected, and
+                    // reported in the replica's status bits
+                    errbits |= 2u;
+                } else if (delta < 0.0f) {
                     acc = 1;
                 } else {
                     // u = w / 2^32 < boltz  <=>  w < boltz 2^32, exact in float (power-of-two
@@ -1629,8 +1633,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     const unsigned long long thr = (unsigned long long)ceilf(boltz * 4294967296.0f);
                     acc = ((unsigned long long)mv.w_metro < thr) ? 2 : 0;
                 }
-                if (!isfinite(dEf.hi))
-                    acc = 0;
                 if (DA && screened) {
                     const double dE = ff_value(dEf), e = dE - s_ds;
                     s_da.stage2_eval++;
@@ -1966,7 +1968,11 @@ __global__ void k_exchange(EngineArgs a, int total_replicas, int steps_per_block
             (1.0 / Ti - 1.0 / Tj) * (a.potential[gi] - a.potential[gj]) * (double)(kKcal / kRgas);
         U4 ctr{(uint32_t)x, 0u, (uint32_t)ti, 0x5245u};
         const U4 o = philox4x32_10(ctr, a.seed_lo ^ 0xB5297A4Du, a.seed_hi ^ (0x68E31DA4u * (uint32_t)(s + 1)));
-        if (u01(o.x) < fmin(1.0, exp(delta))) {
+        if (!isfinite(delta)) {
+            // a non-finite potential takes no part in exchanges; both slots report it
+            atomicOr(&a.errflags[gi], 4u);
+            atomicOr(&a.errflags[gj], 4u);
+        } else if (u01(o.x) < fmin(1.0, exp(delta))) {
             // Replica::exchangeReplicas: swap temperature, label and statistics
             float tf = a.temperature[gi];
             a.temperature[gi] = a.temperature[gj];

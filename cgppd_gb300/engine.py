@@ -42,6 +42,7 @@ _DECL = {
     "cgppd_engine_get_report": (c_int, [c_void_p, c_int, c_int, P(c_float), P(c_int)]),
     "cgppd_engine_counters": (c_int, [c_void_p, P(ctypes.c_ulonglong), P(ctypes.c_ulonglong)]),
     "cgppd_engine_error_bits": (ctypes.c_uint, [c_void_p]),
+    "cgppd_engine_replica_error_bits": (c_int, [c_void_p, c_int, P(ctypes.c_uint)]),
     "cgppd_engine_last_launches": (c_int, [c_void_p]),
     "cgppd_engine_launch_shape": (c_int, [c_void_p, P(c_int), P(c_int)]),
     "cgppd_engine_set_resident": (c_int, [c_void_p, c_int]),
@@ -229,6 +230,14 @@ class Engine:
 
     def error_bits(self):
         return _L().cgppd_engine_error_bits(self.h)
+
+    def replica_error_bits(self, sim):
+        """Status bits per replica slot (1 null move, 2 non-finite energy change, 4
+        non-finite potential in an exchange test)."""
+        _, _, R = self.sim_info(sim)
+        out = np.zeros(R, np.uint32)
+        _ok(_L().cgppd_engine_replica_error_bits(self.h, sim, _p(out, ctypes.c_uint)), "replica_error_bits")
+        return out
 
     def last_launches(self):
         return _L().cgppd_engine_last_launches(self.h)

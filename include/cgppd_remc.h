@@ -152,9 +152,14 @@ int cgppd_engine_get_report(cgppd_engine *e, int sim, int row, float *per_temper
 /* MC steps done and residue-pair terms evaluated by all replicas since creation. */
 int cgppd_engine_counters(cgppd_engine *e, unsigned long long *mc_steps, unsigned long long *pair_evals);
 
-/* OR of the per-replica error bits (1: a move type with no candidate residue was
- * drawn and left the molecule unchanged). */
+/* OR of the per-replica status bits: 1 a move type with no candidate residue was drawn
+ * and left the molecule unchanged; 2 a proposal's energy change was not finite
+ * (non-finite coordinates or energies) and the move was rejected; 4 an exchange test
+ * met a non-finite potential and the pair did not exchange. */
 unsigned cgppd_engine_error_bits(cgppd_engine *e);
+
+/* The same bits per replica of simulation `sim` (out: [n_replicas], replica-slot order). */
+int cgppd_engine_replica_error_bits(cgppd_engine *e, int sim, unsigned *out);
 
 /* Kernel launches enqueued by the last cgppd_engine_run call. */
 int cgppd_engine_last_launches(const cgppd_engine *e);

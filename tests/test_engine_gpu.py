@@ -245,3 +245,36 @@ def test_counters_and_launches():
     assert steps == 2 * 30
     assert pairs == 2 * 30 * 76 * 76
     assert e.last_launches() == 6
+
+
+def test_non_finite_coordinates_are_reported_not_propagated():
+    # a replica whose coordinates turn non-finite (injected on the host) rejects every
+    # move and takes no part in exchanges; the others run on, and each slot reports
+    # its own status bits (2: non-finite energy change, 4: non-finite exchange test)
+    wl = workloads.make("c0")
+    sim = subset(wl, 4)
+    e = engine_for(wl, [sim], cluster=2)
+    e.run(1, 20)
+    bad = 2
+    xyz, rel, cen = e.state(0, bad)
+    xyz[0, 0] = np.nan
+    rel[0, 0] = np.nan
+    e.set_state(0, bad, xyz, rel, cen)
+    e.recompute(write_state=True)
+    before = e.replicas(0)
+    e.run(3, 40)
+    after = e.replicas(0)
+    bits = e.replica_error_bits(0)
+    assert bits[bad] & 2
+    for r in range(4):
+        if r != bad:
+            assert not (bits[r] & 2), (r, bits)
+            assert np.isfinite(after["potential"][r])
+    # the bad replica's temperature never moved and its coordinates never changed
+    assert after["temperature"][bad] == before["temperature"][bad]
+    xyz2, _, _ = e.state(0, bad)
+    assert np.array_equal(np.isnan(xyz2), np.isnan(xyz))
+    assert np.array_equal(xyz2[~np.isnan(xyz2)], xyz[~np.isnan(xyz)])
+    # its ladder neighbours saw the non-finite exchange test
+    assert bits[bad] & 4
+    assert e.error_bits() & 6 == 6
