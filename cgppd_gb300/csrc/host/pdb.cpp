@@ -1,6 +1,9 @@
 // pdb.cpp -- see pdb.h.
 #include "pdb.h"
 
+#include "../status.h"
+#include "cgppd_pdb.h"
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -140,3 +143,38 @@ void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float 
 }
 
 }  // namespace cgppd
+
+extern "C" int cgppd_pdb_read(const char *path, const AminoAcids *a, int capacity, float *xyz, int *types,
+                              char *chain_ids, int *res_seq, int *chain_index, int *num_chains)
+{
+    if (!path || !a)
+        return cgppd_fail("cgppd_pdb_read: path and residue table are required");
+    std::vector<cgppd::PdbResidue> res;
+    int chains = 0;
+    try {
+        res = cgppd::read_pdb(path, *a, &chains);
+    } catch (const char *msg) {
+        return cgppd_fail(msg);
+    }
+    const int n = (int)res.size();
+    if (capacity >= n) {
+        for (int i = 0; i < n; ++i) {
+            if (xyz) {
+                xyz[3 * i] = res[i].x;
+                xyz[3 * i + 1] = res[i].y;
+                xyz[3 * i + 2] = res[i].z;
+            }
+            if (types)
+                types[i] = res[i].type;
+            if (chain_ids)
+                chain_ids[i] = res[i].chain;
+            if (res_seq)
+                res_seq[i] = res[i].res_seq;
+            if (chain_index)
+                chain_index[i] = res[i].chain_index;
+        }
+    }
+    if (num_chains)
+        *num_chains = chains;
+    return n;
+}

@@ -97,3 +97,66 @@ def test_repulsive_crowding_key(argdir):
     rc, p = dump(["x", "tests/crowdfile"], 2 | 8, argdir)
     assert rc == 0, p
     assert p["repulsiveCrowding"] == "1" and p["nonCrowders"] == "2"
+
+
+def read_pdb(path, aa_handle, capacity=4096):
+    L = cgppd_gb300.lib()
+    f = L.cgppd_pdb_read
+    f.restype = ctypes.c_int
+    P = ctypes.POINTER
+    f.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, P(ctypes.c_float), P(ctypes.c_int),
+                  ctypes.c_char_p, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]
+    import numpy as np
+    xyz = np.zeros(3 * capacity, np.float32)
+    types = np.zeros(capacity, np.int32)
+    chains = ctypes.create_string_buffer(capacity)
+    seq = np.zeros(capacity, np.int32)
+    cidx = np.zeros(capacity, np.int32)
+    nch = ctypes.c_int(0)
+    n = f(str(path).encode(), aa_handle, capacity, xyz.ctypes.data_as(P(ctypes.c_float)),
+          types.ctypes.data_as(P(ctypes.c_int)), chains, seq.ctypes.data_as(P(ctypes.c_int)),
+          cidx.ctypes.data_as(P(ctypes.c_int)), ctypes.byref(nch))
+    if n < 0:
+        buf = ctypes.create_string_buffer(512)
+        L.cgppd_get_last_error(buf, 512)
+        return n, buf.value.decode()
+    return n, dict(xyz=xyz[:3 * n].reshape(n, 3), types=types[:n], chains=chains.raw[:n].decode(), seq=seq[:n],
+                   chain_index=cidx[:n], num_chains=nch.value)
+
+
+@pytest.mark.parametrize("case", ["good", "unknown_residue", "no_ca_records", "missing_file"])
+def test_pdb_reader(tmp_path, refdata, case):
+    # the reading part of Molecule::initFromPDB (src/Molecule.cpp:506-612); bad files
+    # fail with a message instead of indexing the tables with -1
+    # (src/AminoAcids.cpp:145-181)
+    from helpers import write_reference_data_dir
+    write_reference_data_dir(str(tmp_path), refdata)
+    L = cgppd_gb300.lib()
+    a = L.cgppd_aminoacids_create()
+    d = tmp_path / "data"
+    assert L.cgppd_aminoacids_load(a, str(d / "AminoAcids").encode(), str(d / "pair_potentials_MJ1996").encode()) == 0
+    ubq = d / "application" / "ubq.pdb"
+    lines = ubq.read_text().splitlines()
+    try:
+        if case == "good":
+            n, r = read_pdb(ubq, a)
+            gold = refdata["pdbs"]["application/ubq"]["residues"]
+            assert n == len(gold) == 76 and r["num_chains"] == 1
+            assert r["seq"][0] == 1 and r["seq"][-1] == 76
+            assert all(t >= 0 for t in r["types"])
+            return
+        if case == "unknown_residue":
+            k = next(i for i, ln in enumerate(lines) if ln.startswith("ATOM") and ln[12:16].strip() == "CA")
+            lines[k] = lines[k][:17] + "XYZ" + lines[k][20:]
+            ubq.write_text("\n".join(lines) + "\n")
+            expect = "Unknown residue name"
+        elif case == "no_ca_records":
+            ubq.write_text("\n".join(ln for ln in lines if not ln.startswith("ATOM")) + "\n")
+            expect = "No C-alpha records"
+        else:
+            ubq.unlink()
+            expect = "Failed to open PDB file"
+        n, msg = read_pdb(ubq, a)
+        assert n == -1 and expect in msg
+    finally:
+        L.cgppd_aminoacids_destroy(a)
