@@ -10,8 +10,11 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <cstdlib>
 #include <memory>
+#include <mutex>
 #include <set>
+#include <string>
 #include <vector>
 
 #include "cgppd_common.cuh"
@@ -602,10 +605,89 @@ static void configure_shape(cgppd_engine *e, int C, int T)
 
 // Autotuner: time k_mc for each candidate launch shape on scratch copies of the mutable
 // state (the real trajectory is not advanced) and keep the fastest.  Results are cached
-// per system shape for the life of the process.
+// per system shape for the life of the process and, when the environment variable
+// CGPPD_TUNING_CACHE names a file, persisted there as JSON lines (one object per tuned
+// shape, with the device name and SM count) so that later processes on the same kind
+// of GPU skip the sweep.
+static std::mutex g_tune_mu;
+
+static std::string device_tag()
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p{};
+    cudaGetDeviceProperties(&p, dev);
+    char buf[320];
+    std::snprintf(buf, sizeof(buf), "%s/%d", p.name, p.multiProcessorCount);
+    std::string s = buf;
+    for (char &c : s)
+        if (c == '"' || c == '\\')
+            c = '_';
+    return s;
+}
+
+static void tune_cache_load(std::map<std::vector<long long>, std::pair<int, int>> &cache)
+{
+    const char *path = std::getenv("CGPPD_TUNING_CACHE");
+    if (!path)
+        return;
+    FILE *f = std::fopen(path, "r");
+    if (!f)
+        return;
+    const std::string dev = device_tag();
+    char line[8192];
+    while (std::fgets(line, sizeof(line), f)) {
+        const char *d = std::strstr(line, "\"device\":\""), *k = std::strstr(line, "\"key\":[");
+        const char *c = std::strstr(line, "\"cluster\":"), *t = std::strstr(line, "\"threads\":");
+        if (!d || !k || !c || !t)
+            continue;
+        d += 10;
+        const char *de = std::strchr(d, '"');
+        if (!de || std::string(d, de) != dev)
+            continue;
+        std::vector<long long> key;
+        const char *q = k + 7;
+        while (*q && *q != ']') {
+            char *end = nullptr;
+            const long long v = std::strtoll(q, &end, 10);
+            if (end == q)
+                break;
+            key.push_back(v);
+            q = end;
+            if (*q == ',')
+                ++q;
+        }
+        const int C = std::atoi(c + 10), T = std::atoi(t + 10);
+        if (!key.empty() && C > 0 && T > 0)
+            cache[key] = std::make_pair(C, T);
+    }
+    std::fclose(f);
+}
+
+static void tune_cache_store(const std::vector<long long> &key, int C, int T)
+{
+    const char *path = std::getenv("CGPPD_TUNING_CACHE");
+    if (!path)
+        return;
+    FILE *f = std::fopen(path, "a");
+    if (!f)
+        return;
+    std::fprintf(f, "{\"format\":1,\"device\":\"%s\",\"key\":[", device_tag().c_str());
+    for (size_t i = 0; i < key.size(); ++i)
+        std::fprintf(f, "%s%lld", i ? "," : "", key[i]);
+    std::fprintf(f, "],\"cluster\":%d,\"threads\":%d}\n", C, T);
+    std::fclose(f);
+}
+
 static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
 {
     static std::map<std::vector<long long>, std::pair<int, int>> cache;
+    static bool loaded = false;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (!loaded) {
+        tune_cache_load(cache);
+        loaded = true;
+    }
     std::vector<long long> key{e->total_replicas, e->max_n, e->max_m, e->max_mol, e->any_flexible, e->resident_pref,
                                fixed_cluster, fixed_threads, e->da};
     for (const auto &s : e->h_sims)
@@ -709,6 +791,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
         return -1;
     configure_shape(e, bc, bt);
     cache[key] = std::make_pair(bc, bt);
+    tune_cache_store(key, bc, bt);
     return 0;
 }
 

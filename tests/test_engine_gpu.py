@@ -278,3 +278,28 @@ def test_non_finite_coordinates_are_reported_not_propagated():
     # its ladder neighbours saw the non-finite exchange test
     assert bits[bad] & 4
     assert e.error_bits() & 6 == 6
+
+
+def test_tuning_cache_persists_across_processes(tmp_path):
+    # CGPPD_TUNING_CACHE: the first process sweeps and records the chosen shape, a second
+    # process on the same GPU model reads it and skips the sweep
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from cgppd_gb300 import engine as eng, workloads\n"
+            "e = eng.from_workload(workloads.make('c4'))\n"
+            "print(len(e.tuning()), *e.launch_shape()[:2])\n" % root)
+    env = dict(os.environ, CGPPD_TUNING_CACHE=str(tmp_path / "tuning.jsonl"))
+    first = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert first.returncode == 0, first.stderr
+    n1, c1, t1 = map(int, first.stdout.split()[-3:])
+    assert n1 > 0
+    lines = (tmp_path / "tuning.jsonl").read_text().splitlines()
+    assert len(lines) == 1 and '"cluster":%d' % c1 in lines[0] and '"threads":%d' % t1 in lines[0]
+    second = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert second.returncode == 0, second.stderr
+    n2, c2, t2 = map(int, second.stdout.split()[-3:])
+    assert (n2, c2, t2) == (0, c1, t1)
+    assert len((tmp_path / "tuning.jsonl").read_text().splitlines()) == 1
