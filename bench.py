@@ -157,7 +157,7 @@ def reference_arm(args):
     sim = wl.sims[0]
     threads = min(cores, len(sim.temperatures))
     # one bench step = a bounded block of MC steps of all replicas
-    per = max(1.0, args.cpu_seconds / max(1, args.steps))
+    per = max(0.25, args.cpu_seconds / max(1, args.steps))
     rates = []
     for i in range(args.warmup + args.steps):
         rate, steps, R, dt = cpu_port_rate(wl, per if i >= args.warmup else min(per, 2.0), threads)
@@ -458,6 +458,8 @@ def gpu_arm(args):
     if rank == 0 and world == 1 and not args.no_dropin:
         dropin = dropin_leg(args, torch, flush, workloads.make("c2"), peak_tflops)
     achieved = k_pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
+    sfu_achieved = k_pairs * 2 / (k_ms / 1000.0) / 1e9
+    sfu_peak = props.multi_processor_count * 16 * max_mhz * 1e6 / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(prof):
@@ -483,7 +485,11 @@ def gpu_arm(args):
                          "kernel": "k_mc_block", "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,
                          "flop_per_pair": FLOP_PER_PAIR,
                          "peak_note": "nominal FP32 pipe: SMs x 128 lanes x 2 x max SM clock (no FP32 figure in "
-                                      "the measured peaks)"},
+                                      "the measured peaks)",
+                         "sfu": {"ops_per_pair": 2, "achieved_gops": sfu_achieved, "peak_gops": sfu_peak,
+                                 "frac": sfu_achieved / sfu_peak,
+                                 "note": "secondary ceiling: rsqrt and ex2 per pair against SMs x 16 MUFU "
+                                         "lanes x max SM clock"}},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "surrogate": sur, "dropin": dropin,
         }
