@@ -10,7 +10,8 @@ and delayed-acceptance screening inside the engine.
   to the plain engine (stage 1 always passes, stage 2 is the plain test);
 * the error threshold trips the fallback to the plain test, and a wildly wrong network
   leaves the running totals exact;
-* training lowers the held-out error.
+* training lowers the held-out error, and the trained network's first stage saves exact
+  pair work relative to the plain engine.
 """
 import numpy as np
 import pytest
@@ -201,4 +202,36 @@ def test_training_lowers_heldout_error():
     assert np.all(np.isfinite(hist))
     assert hist[-1, 1] < hist[0, 1]
     e.close()
+    s.close()
+
+
+def test_trained_surrogate_skips_exact_work():
+    # what the trained network gains over the method without it: its first stage rejects
+    # proposals the exact test would mostly reject too, so fewer exact pair terms are
+    # evaluated per MC step than in the plain engine (no speed claim: the measured
+    # throughput of both is in the bench line's surrogate leg)
+    wl = workloads.make("c4")
+    plain = engine_for(wl, [subset(wl, 8)])
+    s, hist = sg.train_on_engine(plain, 0, n_samples=200_000, blocks=4, steps_per_block=200, epochs=4, batch=8192)
+    assert hist[-1, 1] < hist[0, 1]
+    s0, p0 = plain.counters()
+    plain.run(2, 200)
+    plain.synchronize()
+    s1, p1 = plain.counters()
+    plain_per_step = (p1 - p0) / (s1 - s0)
+    da = engine_for(wl, [subset(wl, 8)])
+    assert sg.attach(da, s, rmse_threshold=1e30) == 1
+    a0, q0 = da.counters()
+    da.run(2, 200)
+    da.synchronize()
+    a1, q1 = da.counters()
+    da_per_step = (q1 - q0) / (a1 - a0)
+    st = sg.stats(da, 0)
+    assert st["screening"] == 1 and st["proposals"] == 8 * 400
+    assert st["stage1_reject"] >= 0.05 * st["proposals"], st
+    assert da_per_step <= 0.95 * plain_per_step, (da_per_step, plain_per_step)
+    # the running totals stay exact whatever the first stage decides
+    assert np.allclose(da.recompute(False), da.replicas(0)["potential"], rtol=1e-6, atol=1e-6)
+    plain.close()
+    da.close()
     s.close()
