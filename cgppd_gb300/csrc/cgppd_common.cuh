@@ -58,6 +58,18 @@ __device__ __forceinline__ float min_image(float d, float L, float invL)
     return fmaf(-L, rintf(d * invL), d);
 }
 
+// 1/sqrt(r2) on the SFU (PTX rsqrt.approx.ftz.f32, max relative error 2^-22.9) for the
+// pair terms: a residue pair closer than 1e-19 A does not occur, and the error stays two
+// orders below the 1e-5 energy bound.  (A Newton step on top, as rsqrt_refined does,
+// lengthens each pair's dependency chain by four operations: 7-13 % of the MC kernel's
+// throughput.)
+__device__ __forceinline__ float rsqrt_sfu(float r2)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(r2));
+    return y;
+}
+
 // 1/sqrt(r2) with one Newton step on top of the MUFU estimate (~0.5 ulp).
 __device__ __forceinline__ float rsqrt_refined(float r2)
 {

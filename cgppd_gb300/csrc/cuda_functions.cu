@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
                 const float dyy = min_image(py.y - px.y, L, invL);
                 const float dz = min_image(py.z - px.z, L, invL);
                 const float r2 = fmaf(dx, dx, fmaf(dyy, dyy, dz * dz));
-                const float inv_r = rsqrt_refined(r2);
+                const float inv_r = rsqrt_sfu(r2);
                 const float r = r2 * inv_r;
                 float lt = lj_term(erow[__float_as_int(xm.y)], (ys + px.w) * 0.5f, inv_r * inv_r);
                 float dt = dh_term(yq * xm.x, r, inv_r);

@@ -360,7 +360,7 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
     const float dy = min_image(a.y - b.y, L, invL);
     const float dz = min_image(a.z - b.z, L, invL);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float inv_r = rsqrt_refined(r2);
+    const float inv_r = rsqrt_sfu(r2);
     const float r = r2 * inv_r;
     const float m4e = table[__float_as_int(qa.y) * kTableStride + __float_as_int(qb.y)];
     const float so = (a.w + b.w) * inv_r;  // sigma_ij / r
@@ -382,7 +382,7 @@ __device__ __forceinline__ float crowder_kcal(float4 a, float4 b, float L, float
     const float dy = min_image(a.y - b.y, L, invL);
     const float dz = min_image(a.z - b.z, L, invL);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float inv_r = rsqrt_refined(r2);
+    const float inv_r = rsqrt_sfu(r2);
     const float s = 6.0f * inv_r;
     const float s2 = s * s;
     const float s6 = s2 * s2 * s2;
