@@ -54,8 +54,11 @@ __device__ __forceinline__ double ff_value(const FF &a) { return (double)a.hi + 
 // ------------------------------------------------------------------ geometry
 __device__ __forceinline__ float min_image(float d, float L, float invL)
 {
-    // d - L*rint(d/L) (src/CudaFunctions.cu:321-333); L == 0 means no periodic box.
-    return fmaf(-L, rintf(d * invL), d);
+    // d - L*rint(d/L) (src/CudaFunctions.cu:321-333); L == 0 means no periodic box.  The
+    // nearest integer to d/L comes from adding and removing 1.5 * 2^23 (exact for
+    // |d/L| < 2^22), which keeps the whole term on the FMA pipe.
+    const float k = __fadd_rn(__fmaf_rn(d, invL, 12582912.0f), -12582912.0f);
+    return fmaf(-L, k, d);
 }
 
 // 1/sqrt(r2) on the SFU (PTX rsqrt.approx.ftz.f32, max relative error 2^-22.9) for the
