@@ -1,6 +1,6 @@
 // engine_kernels.cu -- device side of the batched replica-exchange Monte Carlo engine.
 //
-// k_mc<RES, DA>: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
+// k_mc<RES, DA, QF>: one thread-block cluster per replica runs `nsteps` Monte Carlo steps of
 // that replica with no inter-replica traffic (replicas are independent between
 // exchanges); every replica of every simulation is in the one launch.  A step restates
 // Replica::MCSearch (src/Replica.cpp:350-414):
@@ -31,10 +31,14 @@
 //
 // DA = true: delayed-acceptance screening with the learned surrogate (see below).
 //
-// k_exchange: one thread per simulation performs the even/odd temperature exchange of
+// QF = true: a rigid mover is also kept in charged-first order, and the pair loop takes
+// the Debye-Hueckel term for its charged residues only (most residues carry no charge).
+//
+// k_exchange: one warp per simulation performs the even/odd temperature exchange of
 // Simulation::run (src/Simulation.cpp:770-795), the per-temperature bookkeeping of
 // Replica::fraction_bound / acceptance_ratio (src/Replica.cpp:1095-1122) and the
 // surrogate's fallback check.
+#include <array>
 #include <cooperative_groups.h>
 
 #include "cgppd_common.cuh"
@@ -64,10 +68,10 @@ struct MoveDesc {
 };
 
 struct SmemLayout {
-    int table, mols, ipos, irel, iexcl, idisp, iq, ej, rowp, row;    // always
+    int table, mols, ipos, irel, iexcl, idisp, iq, ipq, iqq, ej, rowp, row;  // always
     int rcv;                                                         // clusters: pushed partial rows
     int lst[12];                                                     // resident + flexible: static lists
-    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM;                        // resident only
+    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM, QP;                    // resident only
     int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
     int total;
 };
@@ -121,12 +125,14 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     L.iexcl = off;  off += 16 * max_mol;
     L.idisp = off;  off += 16 * max_mol;
     L.iq = off;     off = align16(off + 8 * max_mol);
+    L.ipq = off;    off += 16 * max_mol;  // the rigid mover in charged-first order
+    L.iqq = off;    off = align16(off + 8 * max_mol);
     L.ej = off;     off = align16(off + 8 * slice);
     L.rowp = off;   off = align16(off + 8 * (max_m + 1));
     L.row = off;    off = align16(off + 8 * (max_m + 1));
     // [2 step parities][C source ranks][max_m + 1] (last entry: internal energy)
     L.rcv = off;    off = align16(off + (C > 1 ? 2 * C * (max_m + 1) * 8 : 0));
-    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = 0;
+    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = L.QP = 0;
     if (resident) {
         L.P = off;      off += 16 * max_n;
         L.Q = off;      off += 16 * max_n;
@@ -136,6 +142,7 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
         L.EM = off;     off = align16(off + 8 * max_m * max_m);
         L.INTRA = off;  off = align16(off + 8 * max_m);
         L.ROWSUM = off; off = align16(off + 8 * max_m);
+        L.QP = off;     off = align16(off + 2 * max_n);  // charged-first positions
     }
     for (int k = 0; k < 12; ++k)
         L.lst[k] = 0;
@@ -353,6 +360,7 @@ __device__ __forceinline__ float3 normalized(float x, float y, float z)
 // (q*sqrt(DHF), type) in qa/qb.  `table` holds -4 Eij (kcal/mol): the LJ term is
 // u = (-4 Eij) s6 (s6 - 1), and 2 Eij - u on the repulsive branch (Eij > 0, s6 > 1/2),
 // the same values as lj_term with one multiplication less (power-of-two scaling).
+template <bool DH = true>
 __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float *table, float L,
                                            float invL)
 {
@@ -369,6 +377,8 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
     float u = m4e * s6 * (s6 - 1.0f);
     if (m4e < 0.0f && s6 > 0.5f)
         u = fmaf(-0.5f, m4e, -u);
+    if (!DH)  // one of the pair uncharged: no Debye-Hueckel term
+        return u;
     return u + qa.x * qb.x * ex2_sfu(r * (-kLog2e / kXi)) * inv_r;
 }
 
@@ -958,7 +968,7 @@ __device__ void da_init_matrix(DaView &v, const DevMol *mols, const float4 *Q, c
 
 // ------------------------------------------------------------------ MC kernel
 
-template <bool RES, bool DA>
+template <bool RES, bool DA, bool QF>
 __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1007,6 +1017,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     int4 *s_iexcl = reinterpret_cast<int4 *>(smem + Ly.iexcl);
     float4 *s_disp = reinterpret_cast<float4 *>(smem + Ly.idisp);
     float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
+    float4 *s_ipq = reinterpret_cast<float4 *>(smem + Ly.ipq);
+    float2 *s_iqq = reinterpret_cast<float2 *>(smem + Ly.iqq);
+    unsigned short *s_qpos = reinterpret_cast<unsigned short *>(smem + Ly.QP);
     float2 *s_ej = reinterpret_cast<float2 *>(smem + Ly.ej);
     FF *s_rowp = reinterpret_cast<FF *>(smem + Ly.rowp);
     FF *s_row = reinterpret_cast<FF *>(smem + Ly.row);
@@ -1051,6 +1064,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             sP[i] = make_float4(p.x, p.y, p.z, sr.x);
             sQ[i] = make_float4(q.x, q.y, q.z, sr.y);
             sTY[i] = (unsigned char)__float_as_int(sr.z);
+            if (QF)
+                s_qpos[i] = a.rqpos[S.res_off + i];
         }
         if (a.any_flexible) {
             int4 *sEX = reinterpret_cast<int4 *>(smem + Ly.EX);
@@ -1294,6 +1309,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             np.w = sr.x;
             s_ipos[i] = np;
             s_irel[i] = nq;
+            if (QF && !flexmol) {  // the rigid mover also in charged-first order (its final positions)
+                const int k = RES ? s_qpos[start + i] : a.rqpos[S.res_off + start + i];
+                s_ipq[k] = np;
+                s_iqq[k] = make_float2(sr.y, sr.z);
+            }
         }
         __syncthreads();
         if (type == kFlex && !nullm) {
@@ -1360,6 +1380,12 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         // g lanes per j (each takes every g-th i), floor(32 / g) groups of lanes per warp;
         // the lanes past the last whole group idle
         const int g = s_mols[m].pair_lanes, jw = 32 / g;
+        // a rigid mover is read in charged-first order: its first nqm residues take the
+        // full pair term, the rest the Lennard-Jones part alone (no charge, no Debye-Hueckel)
+        const bool qfirst = QF && !flexmol;
+        const float4 *ipv = qfirst ? s_ipq : s_ipos;
+        const float2 *iqv = qfirst ? s_iqq : s_iq;
+        const int nqm = qfirst ? s_mols[m].nq : n;
         // repulsive crowding: pairs with a crowder (j >= cstart, or a crowder mover) take
         // the crowder term
         const int cstart = (S.crowd_start >= 0) ? S.crowd_start : 0x7fffffff;
@@ -1392,7 +1418,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 float p0 = 0.f;
                 int cntp = 0;
                 for (int i = sub; i < n; i += g) {
-                    p0 += crowder_kcal(s_ipos[i], pj, L, invL);
+                    p0 += crowder_kcal(ipv[i], pj, L, invL);
                     if (++cntp == 32) {
                         ff_add(acc, p0);
                         p0 = 0.f;
@@ -1407,11 +1433,24 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 // into the float-float accumulator every 32 terms
                 float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
                 int i = sub, cntp = 0;
+                for (; i + 3 * g < nqm; i += 4 * g) {
+                    p0 += pair_kcal(ipv[i], iqv[i], rj, qj, s_table, L, invL);
+                    p1 += pair_kcal(ipv[i + g], iqv[i + g], rj, qj, s_table, L, invL);
+                    p2 += pair_kcal(ipv[i + 2 * g], iqv[i + 2 * g], rj, qj, s_table, L, invL);
+                    p3 += pair_kcal(ipv[i + 3 * g], iqv[i + 3 * g], rj, qj, s_table, L, invL);
+                    if (++cntp == 8) {
+                        ff_add(acc, (p0 + p1) + (p2 + p3));
+                        p0 = p1 = p2 = p3 = 0.f;
+                        cntp = 0;
+                    }
+                }
+                for (; i < nqm; i += g)
+                    p0 += pair_kcal(ipv[i], iqv[i], rj, qj, s_table, L, invL);
                 for (; i + 3 * g < n; i += 4 * g) {
-                    p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
-                    p1 += pair_kcal(s_ipos[i + g], s_iq[i + g], rj, qj, s_table, L, invL);
-                    p2 += pair_kcal(s_ipos[i + 2 * g], s_iq[i + 2 * g], rj, qj, s_table, L, invL);
-                    p3 += pair_kcal(s_ipos[i + 3 * g], s_iq[i + 3 * g], rj, qj, s_table, L, invL);
+                    p0 += pair_kcal<false>(ipv[i], iqv[i], rj, qj, s_table, L, invL);
+                    p1 += pair_kcal<false>(ipv[i + g], iqv[i + g], rj, qj, s_table, L, invL);
+                    p2 += pair_kcal<false>(ipv[i + 2 * g], iqv[i + 2 * g], rj, qj, s_table, L, invL);
+                    p3 += pair_kcal<false>(ipv[i + 3 * g], iqv[i + 3 * g], rj, qj, s_table, L, invL);
                     if (++cntp == 8) {
                         ff_add(acc, (p0 + p1) + (p2 + p3));
                         p0 = p1 = p2 = p3 = 0.f;
@@ -1419,7 +1458,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     }
                 }
                 for (; i < n; i += g)
-                    p0 += pair_kcal(s_ipos[i], s_iq[i], rj, qj, s_table, L, invL);
+                    p0 += pair_kcal<false>(ipv[i], iqv[i], rj, qj, s_table, L, invL);
                 ff_add(acc, (p0 + p1) + (p2 + p3));
             }
             // segmented tree sum towards the group's first lane: after the step with offset
@@ -2122,6 +2161,17 @@ cudaError_t launch_pose_samples(const EngineArgs &a, const int4 *items, int n, u
     return cudaGetLastError();
 }
 
+// Every instantiation of k_mc a launch can pick: resident or not x delayed acceptance x
+// charged-first mover order (the last only without delayed acceptance).
+static const std::array<const void *, 6> &mc_kernels()
+{
+    static const std::array<const void *, 6> k = {
+        (const void *)k_mc<true, false, false>, (const void *)k_mc<false, false, false>,
+        (const void *)k_mc<true, true, false>,  (const void *)k_mc<false, true, false>,
+        (const void *)k_mc<true, false, true>,  (const void *)k_mc<false, false, true>};
+    return k;
+}
+
 cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps, int threads, size_t smem,
                             cudaStream_t stream)
 {
@@ -2141,26 +2191,27 @@ cudaError_t launch_mc_block(const EngineArgs &a, int total_replicas, int nsteps,
     if (C > 8) {  // 16-CTA clusters are a non-portable size: opt in once per kernel
         static bool allowed = false;
         if (!allowed) {
-            cudaError_t e = cudaFuncSetAttribute(k_mc<true, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_mc<false, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_mc<true, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_mc<false, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            if (e != cudaSuccess)
-                return e;
+            for (const void *f : mc_kernels()) {
+                const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                if (e != cudaSuccess)
+                    return e;
+            }
             allowed = true;
         }
     }
     if (a.da) {
         if (a.resident)
-            return cudaLaunchKernelEx(&cfg, k_mc<true, true>, a, nsteps);
-        return cudaLaunchKernelEx(&cfg, k_mc<false, true>, a, nsteps);
+            return cudaLaunchKernelEx(&cfg, k_mc<true, true, false>, a, nsteps);
+        return cudaLaunchKernelEx(&cfg, k_mc<false, true, false>, a, nsteps);
+    }
+    if (a.qfirst) {
+        if (a.resident)
+            return cudaLaunchKernelEx(&cfg, k_mc<true, false, true>, a, nsteps);
+        return cudaLaunchKernelEx(&cfg, k_mc<false, false, true>, a, nsteps);
     }
     if (a.resident)
-        return cudaLaunchKernelEx(&cfg, k_mc<true, false>, a, nsteps);
-    return cudaLaunchKernelEx(&cfg, k_mc<false, false>, a, nsteps);
+        return cudaLaunchKernelEx(&cfg, k_mc<true, false, false>, a, nsteps);
+    return cudaLaunchKernelEx(&cfg, k_mc<false, false, false>, a, nsteps);
 }
 
 cudaError_t set_mc_smem_limit(size_t smem)
@@ -2171,13 +2222,10 @@ cudaError_t set_mc_smem_limit(size_t smem)
     if (smem <= s_max)
         return cudaSuccess;
     s_max = smem;
-    cudaError_t e = cudaFuncSetAttribute(k_mc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaSuccess;
+    for (const void *f : mc_kernels())
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_init_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return e;

@@ -67,6 +67,7 @@ struct DevMol {
     int tile_off, ntile;         // 32 x 32 intra tiles (ta <= tb) holding an unexcluded pair
     float tors_const;            // sum of V_n over the molecule's torsions (kcal/mol)
     int pair_lanes;              // lanes per other residue in the inter pair loop (set per launch)
+    int nq;                      // charged residues: the inter pair loop takes them first
 };
 
 // Delayed-acceptance counters of one replica slot (not swapped on exchange).
@@ -94,6 +95,7 @@ struct EngineArgs {
     const DevSim *sims;
     const int *rep_sim;          // global replica -> simulation
     const int *rep_order;        // launch order of k_mc: cluster index -> global replica
+    const unsigned short *rqpos; // per residue: its place in the molecule's charged-first order
     const DevMol *mols;
     const float4 *rstat;
     const int4 *rexcl;
@@ -135,6 +137,7 @@ struct EngineArgs {
     int cluster;                 // CTAs per replica
     int resident;                // 1: each CTA keeps its replica's state in shared memory
     int any_flexible;            // some molecule carries internal energy terms
+    int qfirst;                  // 1: k_mc<.., .., true> reads rigid movers charged first
     int max_n;                   // largest N
     int max_m;                   // largest M
     int max_mol;                 // largest molecule
