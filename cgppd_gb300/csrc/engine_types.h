@@ -142,7 +142,7 @@ struct EngineArgs {
     int max_m;                   // largest M
     int max_mol;                 // largest molecule
     int lmax[10];                // largest per-simulation count of each static list
-    // delayed acceptance with the learned surrogate (da != 0: k_mc<.., true> is launched)
+    // delayed acceptance with the learned surrogate (da != 0: k_mc<.., true, false> is launched)
     int da;
     const float *sur_P;          // FP32 master parameters
     const void *sur_wf;          // BF16 Wf[3][256][256] of layers 2..4
