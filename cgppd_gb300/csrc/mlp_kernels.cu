@@ -51,21 +51,45 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
     const uint32_t aaddr = tc05::smem_u32(sA), baddr = tc05::smem_u32(sB);
     constexpr uint32_t idesc = tc05::idesc_bf16_f32(128, kGemmN);
 
-    uint32_t phase = 0;
-    int ok = 1;
-    for (int k0 = kb; k0 < ke; k0 += tc05::kChunkK) {
-        // stage the A (128 rows) and B (256 rows) chunks: 16-byte pieces, 8 per row
+    // software pipeline: the next chunk's global loads are in flight (in registers) while
+    // the tensor cores work on this one; the shared tiles are rewritten only after the
+    // MMAs that read them have completed
+    uint4 ra[8], rb[16];
+    auto load_chunk = [&](int k0) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
-            const uint4 v = *reinterpret_cast<const uint4 *>(g.A + (size_t)(m0 + r) * g.K + k0 + c * 8);
-            *reinterpret_cast<uint4 *>(sA + tc05::tile_offset(r, c)) = v;
+            ra[i] = *reinterpret_cast<const uint4 *>(g.A + (size_t)(m0 + r) * g.K + k0 + c * 8);
         }
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
             const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
-            const uint4 v = *reinterpret_cast<const uint4 *>(g.B + (size_t)r * g.K + k0 + c * 8);
-            *reinterpret_cast<uint4 *>(sB + tc05::tile_offset(r, c)) = v;
+            rb[i] = *reinterpret_cast<const uint4 *>(g.B + (size_t)r * g.K + k0 + c * 8);
+        }
+    };
+    uint32_t phase = 0;
+    int ok = 1;
+    bool pending = false;
+    load_chunk(kb);
+    for (int k0 = kb; k0 < ke; k0 += tc05::kChunkK) {
+        if (pending) {
+            const int done = tc05::mbar_wait(&mbar, phase) ? 1 : 0;
+            phase ^= 1u;
+            tc05::fence_after_sync();
+            ok = __syncthreads_and(done);
+            if (!ok)
+                break;
+        }
+        // stage the A (128 rows) and B (256 rows) chunks: 16-byte pieces, 8 per row
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
+            *reinterpret_cast<uint4 *>(sA + tc05::tile_offset(r, c)) = ra[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
+            *reinterpret_cast<uint4 *>(sB + tc05::tile_offset(r, c)) = rb[i];
         }
         tc05::fence_proxy_async();
         __syncthreads();
@@ -77,13 +101,15 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
                               (k0 > kb) || (kk > 0));
             tc05::mma_commit(&mbar);
         }
-        // the tiles are reused only after the tensor cores have read them
+        pending = true;
+        if (k0 + tc05::kChunkK < ke)
+            load_chunk(k0 + tc05::kChunkK);
+    }
+    if (ok && pending) {  // the accumulator is read only after the last MMAs completed
         const int done = tc05::mbar_wait(&mbar, phase) ? 1 : 0;
         phase ^= 1u;
         tc05::fence_after_sync();
         ok = __syncthreads_and(done);
-        if (!ok)
-            break;
     }
 
     if (ok) {
