@@ -5,7 +5,8 @@
 // K-major, one 128 x 256 tile per CTA (accumulator = 256 TMEM columns x 128 lanes).
 // 64-wide K chunks are staged into shared memory by the CTA's 128 threads in the
 // no-swizzle core-matrix layout (tc05.cuh), then one thread issues four K = 16 MMAs and
-// commits them to an mbarrier.  Epilogues read the accumulator back with tcgen05.ld
+// commits them to an mbarrier; the next chunk's global loads are issued into registers
+// while those MMAs run.  Epilogues read the accumulator back with tcgen05.ld
 // (warp w owns lanes 32w..32w+31 = rows of the tile) and fuse what the layer needs:
 //   kGemmFwd   z = acc + bias -> Z (f32), h = silu(z) -> H (bf16) and H^T (bf16)
 //   kGemmBwd   d = acc * silu'(Zprev) -> dZ (bf16) and dZ^T (bf16)
