@@ -3,11 +3,12 @@
 // The three 256x256 layers run as BF16 GEMMs on the tcgen05 tensor cores with FP32
 // accumulation in tensor memory: C[M x 256] = A[M x K] * B[256 x K]^T, both operands
 // K-major, one 128 x 256 tile per CTA (accumulator = 256 TMEM columns x 128 lanes).
-// 64-wide K chunks are staged into shared memory by the CTA's 128 threads in the
+// 64-wide K chunks are staged into shared memory by the CTA's 256 threads in the
 // no-swizzle core-matrix layout (tc05.cuh), then one thread issues four K = 16 MMAs and
 // commits them to an mbarrier; the next chunk's global loads are issued into registers
 // while those MMAs run.  Epilogues read the accumulator back with tcgen05.ld
-// (warp w owns lanes 32w..32w+31 = rows of the tile) and fuse what the layer needs:
+// (warp w owns lanes 32(w % 4)..+31 = rows of the tile, columns of half w / 4) and
+// fuse what the layer needs:
 //   kGemmFwd   z = acc + bias -> Z (f32), h = silu(z) -> H (bf16) and H^T (bf16)
 //   kGemmBwd   d = acc * silu'(Zprev) -> dZ (bf16) and dZ^T (bf16)
 //   kGemmStore acc -> C[z] (f32 split-K partial, reduced in a fixed order afterwards)
@@ -23,7 +24,9 @@
 namespace cgppd {
 
 constexpr int kGemmN = 256;
-constexpr int kGemmThreads = 128;
+constexpr int kGemmThreads = 256;   // 8 warps: two per TMEM lane quadrant, one per column half
+constexpr int kGemmLoadsA = 128 * 8 / kGemmThreads;     // 16-byte pieces of A per thread and chunk
+constexpr int kGemmLoadsB = kGemmN * 8 / kGemmThreads;  // and of B
 constexpr int kGemmTileA = 128 * tc05::kChunkK * 2;       // 16 KB
 constexpr int kGemmTileB = kGemmN * tc05::kChunkK * 2;    // 32 KB
 // Requested dynamic shared memory: the tiles plus slack so that at most two CTAs share
@@ -55,15 +58,15 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
     // software pipeline: the next chunk's global loads are in flight (in registers) while
     // the tensor cores work on this one; the shared tiles are rewritten only after the
     // MMAs that read them have completed
-    uint4 ra[8], rb[16];
+    uint4 ra[kGemmLoadsA], rb[kGemmLoadsB];
     auto load_chunk = [&](int k0) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < kGemmLoadsA; ++i) {
             const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
             ra[i] = *reinterpret_cast<const uint4 *>(g.A + (size_t)(m0 + r) * g.K + k0 + c * 8);
         }
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < kGemmLoadsB; ++i) {
             const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
             rb[i] = *reinterpret_cast<const uint4 *>(g.B + (size_t)r * g.K + k0 + c * 8);
         }
@@ -83,12 +86,12 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
         }
         // stage the A (128 rows) and B (256 rows) chunks: 16-byte pieces, 8 per row
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < kGemmLoadsA; ++i) {
             const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
             *reinterpret_cast<uint4 *>(sA + tc05::tile_offset(r, c)) = ra[i];
         }
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < kGemmLoadsB; ++i) {
             const int idx = t + kGemmThreads * i, r = idx >> 3, c = idx & 7;
             *reinterpret_cast<uint4 *>(sB + tc05::tile_offset(r, c)) = rb[i];
         }
@@ -114,9 +117,12 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
     }
 
     if (ok) {
-        const int row = m0 + warp * 32 + lane;
-        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int n0 = 0; n0 < kGemmN; n0 += 16) {
+        // warp w reads TMEM lane quadrant w % 4 (rows 32(w % 4) .. +31 of the tile) and
+        // column half w / 4
+        const int quad = warp & 3, chalf = warp >> 2;
+        const int row = m0 + quad * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16);
+        for (int n0 = chalf * (kGemmN / 2); n0 < (chalf + 1) * (kGemmN / 2); n0 += 16) {
             float v[16];
             tc05::tmem_ld16(lane_base + (uint32_t)n0, v);
             if (MODE == kGemmStore) {
