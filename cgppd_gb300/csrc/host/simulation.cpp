@@ -117,7 +117,7 @@ void Simulation::getArgs(int argc, char **argv, bool first_pass)
             break;
         switch (opt) {
         case 'p':
-            std::fprintf(stderr, "cgppd: this build has no OpenGL preview\n");
+            std::fprintf(stderr, "cgppd: no OpenGL preview (headless)\n");
             break;
         case 'q': parameters.skipsimulation = true; break;
         case 't': parameters.threads = std::atoi(optarg); break;
