@@ -19,11 +19,13 @@ from oracle.remc import OracleRemc
 RT = oracle.RT_TO_KCAL
 
 
-def small_crowded(seed=7, rep_crowd=True):
+def small_crowded(seed=7, rep_crowd=True, large=False):
+    # large: proteins of 100+ residues, so the engine reads the mover charged first
     rng = np.random.default_rng(seed)
     sigma_type = rng.uniform(4.5, 7.0, size=21).astype(np.float32)
     table = workloads.contact_table(rng, with_crowder=True, crowder_eps=0.1)
-    sim = workloads.rigid_sim(rng, [30, 24, 36], 60.0, 4, sigma_type, crowders=5, crowder_len=12)
+    lengths, box = ([110, 64], 80.0) if large else ([30, 24, 36], 60.0)
+    sim = workloads.rigid_sim(rng, lengths, box, 4, sigma_type, crowders=5, crowder_len=12)
     sim.repulsive_crowding = rep_crowd
     return table, sim
 

@@ -48,10 +48,10 @@ def test_initial_matrix(cluster):
         assert abs(e.replicas(0)["potential"][r] - tot) <= REL * abs(tot) + 1e-9
 
 
-@pytest.mark.parametrize("resident", [True, False])
-@pytest.mark.parametrize("cluster", [1, 3])
-def test_trajectory_matches_oracle(cluster, resident):
-    table, sim = small_crowded()
+@pytest.mark.parametrize("resident,cluster,large", [(True, 1, False), (False, 1, False), (True, 3, False),
+                                                   (False, 3, False), (True, 2, True), (False, 2, True)])
+def test_trajectory_matches_oracle(cluster, resident, large):
+    table, sim = small_crowded(large=large)
     e, wl = engine(table, sim, cluster=cluster, resident=resident)
     assert e.launch_shape()[:1] == (cluster,) and e.launch_shape()[2] == resident
     o = OracleRemc(sim.molecules, table, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
