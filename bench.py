@@ -1,20 +1,25 @@
 """Benchmark: replica-exchange Monte Carlo throughput on one GB300.
 
-Metric (BASELINE): MC steps/s and residue-pair evaluations/s.  A bench "step" is one
-exchange block of the workload: every replica advances `--block` Monte Carlo steps
-(move, energy of the moved molecule, Metropolis) on the GPU, then one even/odd
-temperature exchange runs.  value = replica MC steps per second over the timed steps.
+Metric: MC steps/s and residue-pair evaluations/s.  A bench "step" is one exchange
+block of the workload: every replica advances `--block` Monte Carlo steps (move, energy
+of the moved molecule, Metropolis) on the GPU, then one even/odd temperature exchange
+runs.  value = replica MC steps per second over the timed steps.
 
-Default workload: the flexible-linker configuration (76 + 10 + 76 residues, one
-chain, 32 replicas 288-450 K, flex moves 30 %), seeded synthetic inputs.  The
-state (a few hundred KB) lives in L2, so every timed step is preceded by an L2
-flush (a 256 MiB write) inside the timed region.
+Default workload: the batched uneven configuration -- 96 independent simulations of
+2-12 rigid molecules with log-uniform lengths 40-400 residues and 8-40 replicas each
+(2,218 replicas, 101,651 residues), seeded synthetic inputs, all in one launch.  Its
+resident state (~110 MB) is below the 129 MB L2, so every timed step is preceded by an
+L2 flush (a 256 MiB write) inside the timed region.  The flexible-linker (c1), crowded
+(c2) and identical-copies (c4) configurations run as extra legs of the same line.
 
 Arms:
   default            the GB300 engine (libcgppd_gb300.so), CUDA-graph replays
   --impl reference   the reference CPU algorithm (full energy recomputation every
                      step, reference precision) timed on this host's cores: the
-                     oracle's port of the reference loop, rank 0 only
+                     oracle's port of the reference loop, rank 0 only.  For the
+                     batched configuration a bench step is one MC step of every
+                     replica of a stratified share of the simulations, so that the
+                     timed steps together sweep every simulation
 Launched with torchrun for N > 1, each rank runs an independent set of replicas
 ("replicas only": the path has no cross-GPU exchange step), value = sum over ranks.
 """
@@ -41,7 +46,9 @@ def parse():
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="c1")
+    p.add_argument("--workload", default="c3")
+    p.add_argument("--legs", default="c1,c2,c4", help="extra workloads timed in the same line ('' for none)")
+    p.add_argument("--leg-blocks", type=int, default=10, help="timed blocks of each extra leg")
     p.add_argument("--block", type=int, default=1000, help="MC steps per exchange block")
     p.add_argument("--cluster", type=int, default=0)
     p.add_argument("--threads", type=int, default=0)
@@ -129,22 +136,55 @@ def reduce_over_ranks(seconds, counts, dist=None, device="cpu"):
 
 # ------------------------------------------------------------------ CPU arm
 
-def cpu_port_rate(wl, seconds, threads):
-    """The oracle's port of the reference CPU loop on the workload's first simulation:
-    replica MC steps per second using `threads` host threads, on a bounded sample."""
-    from oracle.remc import OracleRemc
-    sim = wl.sims[0]
-    o = OracleRemc(sim.molecules, wl.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
-                   sim.move_weights, sim.rigid_rotate_prob, wl.torsion_V, wl.torsion_phase, seed=wl.seed)
-    R = o.R
-    t0 = time.perf_counter()
-    o.run(1, 2, threads=threads)
-    cal = max(time.perf_counter() - t0, 1e-4) / 2.0  # seconds per MC step of all replicas
-    steps = max(4, int(seconds / cal))
-    t0 = time.perf_counter()
-    o.run(1, steps, threads=threads)
-    dt = time.perf_counter() - t0
-    return R * steps / dt, steps, R, dt
+class CpuPort:
+    """The oracle's port of the reference CPU loop (full energy recomputation every MC
+    step, reference precision) over the simulations of a workload.  Every replica runs
+    on its own host thread and the simulations of a sample run concurrently, so the OS
+    spreads the work over all host cores."""
+
+    def __init__(self, wl):
+        from oracle.remc import OracleRemc
+        self.wl = wl
+        self.sims = [OracleRemc(s.molecules, wl.lj_raw, s.box, s.temperatures, s.translate_steps, s.rotate_steps,
+                                s.move_weights, s.rigid_rotate_prob, wl.torsion_V, wl.torsion_phase, seed=wl.seed,
+                                repulsive_crowding=s.repulsive_crowding)
+                     for s in wl.sims]
+        self.cores = os.cpu_count() or 1
+
+    def sample(self, sim_ids, steps=1):
+        """`steps` MC steps of every replica of the simulations `sim_ids`: (replica MC
+        steps, seconds)."""
+        from concurrent.futures import ThreadPoolExecutor
+        sel = [self.sims[i] for i in sim_ids]
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=max(1, len(sel))) as ex:
+            list(ex.map(lambda o: o.run(1, steps, False, threads=o.R), sel))
+        dt = time.perf_counter() - t0
+        return sum(o.R for o in sel) * steps, dt
+
+    def strata(self, k):
+        """k shares of the simulations, each a mix of large and small ones (simulations
+        ranked by pair work per step, dealt round-robin)."""
+        work = [o.R * (o.N * o.N) for o in self.sims]
+        order = sorted(range(len(self.sims)), key=lambda i: -work[i])
+        return [order[j::k] for j in range(k) if order[j::k]]
+
+
+def cpu_sweep(wl, min_seconds):
+    """CPU baseline of the bench line: whole sweeps (one MC step of every replica of every
+    simulation), repeated until `min_seconds` have passed."""
+    port = CpuPort(wl)
+    every = list(range(len(wl.sims)))
+    port.sample([min(every, key=lambda i: port.sims[i].N)])  # warm-up
+    done, secs, sweeps = 0, 0.0, 0
+    while secs < min_seconds or sweeps == 0:
+        n, dt = port.sample(every, 1 if len(every) > 1 else 16)
+        done, secs, sweeps = done + n, secs + dt, sweeps + 1
+    return {"value": done / secs, "unit": "replica MC steps/s", "cores": port.cores, "kind": "port",
+            "sample": "%d sweep(s) of %d MC step(s) of all %d replicas of all %d simulation(s) of the same "
+                      "workload (%.1f s; one host thread per replica)" % (sweeps, 1 if len(every) > 1 else 16,
+                                                                          sum(o.R for o in port.sims), len(every),
+                                                                          secs)}
 
 
 def reference_arm(args):
@@ -153,29 +193,42 @@ def reference_arm(args):
     if rank != 0:
         return
     wl = workloads.make(args.workload)
-    cores = os.cpu_count() or 1
-    sim = wl.sims[0]
-    threads = min(cores, len(sim.temperatures))
-    # one bench step = a bounded block of MC steps of all replicas
-    per = max(0.25, args.cpu_seconds / max(1, args.steps))
-    rates = []
-    for i in range(args.warmup + args.steps):
-        rate, steps, R, dt = cpu_port_rate(wl, per if i >= args.warmup else min(per, 2.0), threads)
-        if i >= args.warmup:
-            rates.append((rate, steps, dt))
-    total_steps = sum(r[0] * r[2] for r in rates)
-    total_t = sum(r[2] for r in rates)
+    port = CpuPort(wl)
+    if len(wl.sims) > 1:
+        # each bench step: one MC step of every replica of one stratum; the timed steps
+        # together cover every simulation (strata repeat when steps > simulations)
+        shares = port.strata(min(args.steps, len(wl.sims)))
+        plan = [(shares[i % len(shares)], 1) for i in range(args.steps)]
+        warm = [([min(range(len(wl.sims)), key=lambda i: port.sims[i].N)], 1)] * args.warmup
+    else:
+        # one simulation: each bench step a bounded block of MC steps of all replicas
+        o = port.sims[0]
+        _, dt = port.sample([0], 2)
+        per = max(0.25, args.cpu_seconds / max(1, args.steps))
+        n = max(4, int(per / max(dt / 2.0, 1e-4)))
+        plan = [([0], n)] * args.steps
+        warm = [([0], max(1, n // 4))] * args.warmup
+    for ids, n in warm:
+        port.sample(ids, n)
+    rates = [port.sample(ids, n) for ids, n in plan]
+    total_steps = sum(r[0] for r in rates)
+    total_t = sum(r[1] for r in rates)
     value = total_steps / total_t
+    covered = sorted(set(i for ids, _ in plan for i in ids))
+    sample = ("%d bench steps, each one MC step of every replica of a stratified share of the %d simulations "
+              "(%d of %d simulations covered, %d replica MC steps in %.1f s; full energy recomputation each "
+              "step, as the reference CPU path)" % (args.steps, len(wl.sims), len(covered), len(wl.sims),
+                                                    total_steps, total_t)) if len(wl.sims) > 1 else \
+        ("%d replicas x %s MC steps per bench step (full energy recomputation each step, as the reference CPU "
+         "path)" % (port.sims[0].R, plan[0][1]))
     out = {"metric": METRIC, "impl": "reference", "value": value, "unit": "replica MC steps/s", "n_gpus": 0,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_t / len(rates),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64/fp32 (reference mix)",
            "data": "synthetic (seeded, configuration shapes)",
-           "config": {"workload": wl.name, "replicas": len(sim.temperatures),
-                      "mc_steps_per_bench_step": [r[1] for r in rates]},
-           "cpu_baseline": {"value": value, "unit": "replica MC steps/s", "cores": threads, "kind": "port",
-                            "sample": "%d replicas x %s MC steps per bench step (full energy recomputation "
-                                      "each step, as the reference CPU path)" % (len(sim.temperatures),
-                                                                                 [r[1] for r in rates])},
+           "config": {"workload": wl.name, "replicas": wl.n_replicas, "simulations": len(wl.sims),
+                      "mc_steps_per_bench_step": [n for _, n in plan]},
+           "cpu_baseline": {"value": value, "unit": "replica MC steps/s", "cores": port.cores, "kind": "port",
+                            "sample": sample},
            "e2e": {"value": value, "unit": "replica MC steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -335,6 +388,91 @@ def dropin_leg(args, torch, flush, wl, peak_tflops):
 
 # ------------------------------------------------------------------ GPU arm
 
+def profile_counters(workload):
+    """Per-launch ncu figures of k_mc on `workload` committed under profiles/ (DRAM
+    traffic, FMA-pipe utilisation), or {}."""
+    path = os.path.join(ROOT, "profiles", "k_mc_counters.json")
+    try:
+        return json.load(open(path)).get(workload, {})
+    except (OSError, ValueError):
+        return {}
+
+
+def kernel_roofline(e, torch, stream, flush, K, peak_tflops, sfu_peak, workload):
+    """The MC block kernel alone (one k_mc launch of K steps of every replica, no exchange)
+    timed with CUDA events on its stream: pair-evals x 80 FLOP / duration."""
+    sh = stream.cuda_stream
+    ktimes = []
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0 = e.counters()[1]
+            a.record(stream)
+            e.run(1, K, False, stream=sh)
+            b.record(stream)
+            b.synchronize()
+            ktimes.append((a.elapsed_time(b), e.counters()[1] - p0))
+    k_ms = float(np.mean([x[0] for x in ktimes]))
+    k_pairs = float(np.mean([x[1] for x in ktimes]))
+    achieved = k_pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
+    sfu = k_pairs * 2 / (k_ms / 1000.0) / 1e9
+    prof = profile_counters(workload)
+    return {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+            "frac": achieved / peak_tflops, "traffic": prof.get("traffic"),
+            "fma_pipe_frac": prof.get("fma_pipe_frac"),
+            "fma_pipe_note": "ncu sm__pipe_fma_cycles_active (fraction of peak sustained) of one k_mc launch, "
+                             "from the committed profile of this workload",
+            "kernel": "k_mc", "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,
+            "flop_per_pair": FLOP_PER_PAIR,
+            "peak_note": "nominal FP32 pipe: SMs x 128 lanes x 2 x max SM clock (no FP32 figure in the measured "
+                         "peaks); 80 FLOP per pair evaluation is the algorithmic count (40 FP32-pipe operations)",
+            "sfu": {"ops_per_pair": 2, "achieved_gops": sfu, "peak_gops": sfu_peak, "frac": sfu / sfu_peak,
+                    "note": "secondary ceiling: rsqrt and ex2 per pair against SMs x 16 MUFU lanes x max SM "
+                            "clock"}}
+
+
+def timed_blocks(e, torch, stream, flush, K, warmup, blocks):
+    """Replica MC steps/s and pair-evals/s of `blocks` exchange blocks after `warmup`
+    untimed ones, an L2 flush before each, CUDA events on the engine's stream."""
+    sh = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            flush.fill_(1.0)
+            e.run(1, K, True, stream=sh)
+    torch.cuda.synchronize()
+    s0, p0 = e.counters()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        for _ in range(blocks):
+            flush.fill_(1.0)
+            e.run(1, K, True, stream=sh)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    s1, p1 = e.counters()
+    return (s1 - s0) / (ms / 1000.0), (p1 - p0) / (ms / 1000.0), ms
+
+
+def leg(name, args, torch, flush, peak_tflops, sfu_peak):
+    """One extra workload of the line: throughput over --leg-blocks blocks and its k_mc
+    roofline."""
+    from cgppd_gb300 import engine as eng
+    from cgppd_gb300 import workloads
+    wl = workloads.make(name)
+    e = eng.from_workload(wl)
+    stream = torch.cuda.Stream()
+    rate, pair_rate, ms = timed_blocks(e, torch, stream, flush, args.block, max(3, args.warmup), args.leg_blocks)
+    roof = kernel_roofline(e, torch, stream, flush, args.block, peak_tflops, sfu_peak, name)
+    shape = e.launch_shape()
+    e.close()
+    return {"workload": wl.name, "replicas": wl.n_replicas, "replica_mc_steps_per_s": rate,
+            "pair_evals_per_s": pair_rate, "blocks": args.leg_blocks, "mc_steps_per_block": args.block,
+            "ms_per_block": ms / args.leg_blocks, "cluster_ctas_per_replica": shape[0], "threads_per_cta": shape[1],
+            "state_in_shared_memory": shape[2], "roofline": roof}
+
+
 def gpu_arm(args):
     import torch
     import cgppd_gb300
@@ -358,6 +496,7 @@ def gpu_arm(args):
     sh = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     K = args.block
+    props = torch.cuda.get_device_properties(local)
 
     def barrier():
         torch.cuda.synchronize()
@@ -388,21 +527,13 @@ def gpu_arm(args):
                                                    dist, "cuda")
     value = all_steps / (ms / 1000.0)
     pair_rate = all_pairs / (ms / 1000.0)
+    clocks = clk.summary()
+    max_mhz = clocks["sm_max_mhz"] or 2070.0
+    peak_tflops = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
+    sfu_peak = props.multi_processor_count * 16 * max_mhz * 1e6 / 1e9
 
-    # kernel-level timing of the MC block (the dominant kernel) with events on its stream
-    ktimes = []
-    with torch.cuda.stream(stream):
-        for _ in range(3):
-            flush.fill_(1.0)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            p0 = e.counters()[1]
-            a.record(stream)
-            e.run(1, K, False, stream=sh)
-            b.record(stream)
-            b.synchronize()
-            ktimes.append((a.elapsed_time(b), e.counters()[1] - p0))
-    k_ms = float(np.mean([x[0] for x in ktimes]))
-    k_pairs = float(np.mean([x[1] for x in ktimes]))
+    # the dominant kernel alone, timed with events on its stream
+    roofline = kernel_roofline(e, torch, stream, flush, K, peak_tflops, sfu_peak, args.workload)
 
     # end to end through the public API with host buffers: upload every replica's state
     # from pinned memory (with a fresh energy evaluation), run the block, download state
@@ -438,60 +569,36 @@ def gpu_arm(args):
         secs, (done,) = reduce_over_ranks(t1 - t0, [e.counters()[0] - s0], dist, "cuda")
         e2e = {"value": done / secs, "unit": "replica MC steps/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = min(os.cpu_count() or 1, len(wl.sims[0].temperatures))
-        rate, steps, Rr, dt = cpu_port_rate(wl, args.cpu_seconds, threads)
-        cpu = {"value": rate, "unit": "replica MC steps/s", "cores": threads, "kind": "port",
-               "sample": "%d replicas x %d MC steps of the same workload (%.1f s)" % (Rr, steps, dt)}
-
-    sur = None
-    if rank == 0 and world == 1 and not args.no_surrogate:
-        sur = surrogate_leg(args, torch, flush)
-
-    props = torch.cuda.get_device_properties(local)
-    clocks = clk.summary()
-    max_mhz = clocks["sm_max_mhz"] or 2070.0
-    peak_tflops = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
-    dropin = None
-    if rank == 0 and world == 1 and not args.no_dropin:
-        dropin = dropin_leg(args, torch, flush, workloads.make("c2"), peak_tflops)
-    achieved = k_pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
-    sfu_achieved = k_pairs * 2 / (k_ms / 1000.0) / 1e9
-    sfu_peak = props.multi_processor_count * 16 * max_mhz * 1e6 / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get(args.workload)
-        except ValueError:
-            traffic = None
     shape = e.launch_shape()
+    tuning = [list(x) for x in e.tuning()]
+    e.close()
+
+    solo = rank == 0 and world == 1
+    cpu = cpu_sweep(wl, args.cpu_seconds) if solo and not args.no_cpu_baseline else None
+    legs = {}
+    if solo:
+        for name in [x for x in args.legs.split(",") if x and x != args.workload]:
+            legs[name] = leg(name, args, torch, flush, peak_tflops, sfu_peak)
+    sur = surrogate_leg(args, torch, flush) if solo and not args.no_surrogate else None
+    dropin = dropin_leg(args, torch, flush, workloads.make("c2"), peak_tflops) \
+        if solo and not args.no_dropin else None
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "replica MC steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded, configuration shapes)",
-            "config": {"workload": wl.name, "replicas": R, "mc_steps_per_bench_step": K,
+            "config": {"workload": wl.name, "simulations": len(wl.sims), "replicas": R,
+                       "residues": sum(s.n_residues for s in wl.sims), "mc_steps_per_bench_step": K,
                        "exchange": "after every block", "l2": "256 MiB flush before every timed step, inside the "
                                                              "timed region", "cluster_ctas_per_replica": shape[0],
-                       "threads_per_cta": shape[1], "state_in_shared_memory": shape[2], "parallelism": "replicas on one GPU" if world == 1 else
+                       "threads_per_cta": shape[1], "state_in_shared_memory": shape[2],
+                       "parallelism": "replicas on one GPU" if world == 1 else
                        "dp%d (independent replica sets)" % world},
             "pair_evals_per_s": pair_rate,
-            "autotune_us_per_mc_step": [list(x) for x in e.tuning()],
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
-                         "frac": achieved / peak_tflops, "traffic": traffic,
-                         "kernel": "k_mc_block", "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,
-                         "flop_per_pair": FLOP_PER_PAIR,
-                         "peak_note": "nominal FP32 pipe: SMs x 128 lanes x 2 x max SM clock (no FP32 figure in "
-                                      "the measured peaks)",
-                         "sfu": {"ops_per_pair": 2, "achieved_gops": sfu_achieved, "peak_gops": sfu_peak,
-                                 "frac": sfu_achieved / sfu_peak,
-                                 "note": "secondary ceiling: rsqrt and ex2 per pair against SMs x 16 MUFU "
-                                         "lanes x max SM clock"}},
+            "autotune_us_per_mc_step": tuning,
+            "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "surrogate": sur, "dropin": dropin,
+            "legs": legs, "surrogate": sur, "dropin": dropin,
         }
         print(json.dumps(out))
     if dist:

@@ -490,38 +490,35 @@ constexpr size_t kNoAllocBytes = 512 + 2 * sizeof(double) * kNoAllocMaxCtas;  //
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_addr[kMaxDevices] = {nullptr};  // device address of the array, per device
+// Calls on one device share that device's array and are serialised; each device has
+// its own copy of the array, so calls on different devices do not wait for each other.
+std::mutex g_noalloc_mu[kMaxDevices];
 
 // In host code g_noalloc_scratch names a host-side stand-in, not device memory; the
-// kernel needs the device address, looked up once per device with that device current.
-unsigned char *noalloc_scratch(int dev)
+// kernel needs the device address, looked up with the device current.  The lookup
+// allocates nothing and is repeated on every call, so the address stays valid after a
+// cudaDeviceReset (which reloads the module, possibly elsewhere); the first lookup on a
+// device also loads the library's device code there.
+unsigned char *noalloc_scratch()
 {
-    if (dev < 0 || dev >= kMaxDevices) {
-        cgppd_fail("CUDA_EonDevice_noalloc: device ordinal above 63");
+    void *p = nullptr;
+    if (cgppd_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "CUDA_EonDevice_noalloc set-up") != 0)
         return nullptr;
-    }
-    if (g_noalloc_addr[dev] == nullptr) {
-        void *p = nullptr;
-        if (cgppd_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "CUDA_EonDevice_noalloc set-up") != 0)
-            return nullptr;
-        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
-    }
-    return g_noalloc_addr[dev];
+    return static_cast<unsigned char *>(p);
 }
 
 }  // namespace
 
 extern "C" {
 
-// Same arguments and result as CUDA_EonDevice.  The first call on a device performs
-// the one-time set-up (the device address of the static scratch) and should come
-// before any stream capture.  datasetSize above 16384 residues is rejected with an
-// error (result 0).  Every call shares the one array and leaves the last call's data
-// in it; the ticket and error flags are cleared before each launch.  Two calls whose
-// kernels overlap on the GPU would race on the array: this function holds a
-// process-wide lock and returns only after its kernel and result copy have finished,
-// so calls made through it do not overlap.
+// Same arguments and result as CUDA_EonDevice.  The first call on a device loads the
+// library's device code there if nothing else has, and should come before any stream
+// capture.  datasetSize above 16384 residues is rejected with an error (result 0).
+// Every call on a device shares that device's array and leaves the last call's data in
+// it; the ticket and error flags are cleared before each launch.  Two calls whose
+// kernels overlap on the GPU would race on the array: this function holds a per-device
+// lock and returns only after its kernel and result copy have finished, so calls made
+// through it on one device do not overlap.
 void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *residueCount,
                             int *moleculePositions, int *moleculeCount, float *LJPotentials, double *result,
                             int blockSize, int datasetSize, int sharedMemSize)
@@ -535,8 +532,12 @@ void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *
         cgppd_fail("CUDA_EonDevice_noalloc: datasetSize exceeds the 16384-residue limit of its static scratch");
         return;
     }
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
     const int dev = current_device();
+    if (dev < 0 || dev >= kMaxDevices) {
+        cgppd_fail("CUDA_EonDevice_noalloc: device ordinal above 63");
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu[dev]);
     const float *table = nullptr;
     {
         std::lock_guard<std::mutex> tlock(g_mu);
@@ -546,7 +547,7 @@ void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *
         cgppd_fail("CUDA_EonDevice_noalloc: no contact table bound (call bindLJTexture first)");
         return;
     }
-    unsigned char *base = noalloc_scratch(dev);
+    unsigned char *base = noalloc_scratch();
     if (base == nullptr)
         return;
     Scratch s;

@@ -1371,6 +1371,16 @@ extern "C" int cgppd_engine_restore(cgppd_engine *e, const char *path)
     std::fclose(fp);
     if (rc != 0 || !ok)
         return cgppd_fail("cgppd_engine_restore: truncated or mismatched checkpoint");
+    // rows past the checkpoint's capacity held this engine's earlier run: clear them, as
+    // in the engine that wrote the checkpoint (report rows start zeroed)
+    if ((int)cap < e->report_capacity) {
+        const size_t rows = (size_t)(e->report_capacity - (int)cap);
+        if (cgppd_check(cudaMemset(e->d_report.ptr + cap * e->total_replicas, 0,
+                                   sizeof(float4) * rows * e->total_replicas), "restore clear") != 0 ||
+            cgppd_check(cudaMemset(e->d_exch_report.ptr + cap * e->sims.size(), 0,
+                                   sizeof(int2) * rows * e->sims.size()), "restore clear") != 0)
+            return -1;
+    }
     return 0;
 }
 

@@ -47,7 +47,10 @@ void CUDA_EonDeviceNC(float4 *residuePositions, float4 *residueMeta, int *residu
 
 /* Replaces CUDA_EonDevice_async (src/CudaFunctions.cu:176-190, src/cudaExterns.h:42):
  * enqueue the energy on `stream`; device_result (resultSize*resultSize floats) receives
- * the total in element 0 and zeros elsewhere, so the caller's host sum is unchanged. */
+ * the total in element 0 and zeros elsewhere, so the caller's host sum is unchanged.
+ * Like the reference's asynchronous call it reports nothing back to the host: a residue
+ * type outside 0..19 is read as type 0 without an error (the synchronous entry points
+ * check the types and fail on such input). */
 void CUDA_EonDevice_async(float4 *residuePositions, float4 *residueMeta, int *residueCount, int *moleculePositions,
                           int *moleculeCount, float *LJPotentials, float *device_result, int resultSize,
                           int blockSize, int datasetSize, int sharedMemSize, cudaStream_t stream);
@@ -69,10 +72,12 @@ void unbindLJTexture(void);
  * stay free of allocation calls): same arguments and result, but its scratch is a
  * static 132,608-byte device array owned by the library, so it calls no cudaMalloc or
  * cudaFree.  datasetSize is limited to 16384 residues (larger sizes are rejected with
- * an error and *result = 0).  The first call on a device looks up the array's device
- * address (one-time set-up) and should come before any stream capture.  All calls
- * share the array; calls whose kernels overlapped on the GPU would race, so this
- * function serialises its own calls and returns after its kernel has finished. */
+ * an error and *result = 0).  Every call looks up the array's device address on the
+ * current device (a lookup allocates nothing, and stays right after cudaDeviceReset);
+ * the first call on a device may load the library's device code there and should come
+ * before any stream capture.  All calls on a device share that device's array; calls
+ * whose kernels overlapped on the GPU would race, so this function serialises its own
+ * calls per device and returns after its kernel has finished. */
 void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *residueCount,
                             int *moleculePositions, int *moleculeCount, float *LJPotentials, double *result,
                             int blockSize, int datasetSize, int sharedMemSize);

@@ -10,6 +10,9 @@ oracle/ref_harness.cpp.  Output goes only to oracle/_ref/ (git-ignored).  The MC
 it is not built.
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+
+REFERENCE_ROOT defaults to $CGPPD_REFERENCE_DIR, else a directory named `reference`
+beside the repository checkout; without either nothing is built.
 """
 import os
 import subprocess
@@ -22,7 +25,20 @@ UNITS = ["Potential", "Residue", "AminoAcids", "AminoAcid", "Geometry", "Quatern
          "TorsionalLookupMatrix"]
 
 
-def build(ref_root="/root/reference"):
+def reference_root():
+    """The reference tree: $CGPPD_REFERENCE_DIR, else `reference` beside the repository
+    checkout, else None."""
+    env = os.environ.get("CGPPD_REFERENCE_DIR")
+    if env:
+        return env if os.path.isdir(env) else None
+    sib = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return sib if os.path.isdir(os.path.join(sib, "src")) else None
+
+
+def build(ref_root=None):
+    ref_root = ref_root or reference_root()
+    if ref_root is None:
+        return None
     src = os.path.join(ref_root, "src")
     if not os.path.isdir(src):
         return None
@@ -39,4 +55,4 @@ def build(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -235,7 +235,11 @@ def remc_outputs(ref, arch):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    from oracle.build_ref import reference_root
+    ref = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if ref is None:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set CGPPD_REFERENCE_DIR)")
     recs = parse_amino_acids(os.path.join(ref, "data/AminoAcids"))
     lj = parse_lj_table(os.path.join(ref, "data/pair_potentials_MJ1996"), recs)
     V, S = parse_torsions(os.path.join(ref, "data/torsional_pair_potentials"), recs)

@@ -60,3 +60,23 @@ def test_restore_rejects_another_system(tmp_path):
         b.restore(path)
     a.close()
     b.close()
+
+
+def test_restore_clears_report_rows_past_the_checkpoint(tmp_path):
+    # an engine that already wrote more report rows than the checkpoint holds shows, after
+    # the restore, the checkpoint's rows and then zeros -- never its own earlier rows
+    wl = workloads.make("c4")
+    a = make(wl, 3, 1)
+    a.run(1, 40)
+    path = tmp_path / "state.ck"
+    a.checkpoint(path)
+    b = make(wl, 3, 1)
+    b.run(6, 40)
+    assert np.any(b.report(0, 4)[0] != 0)
+    b.restore(path)
+    assert np.array_equal(b.report(0, 0)[0], a.report(0, 0)[0], equal_nan=True)
+    for row in range(2, 6):
+        rep, ex = b.report(0, row)
+        assert np.all(rep == 0) and tuple(ex) == (0, 0), (row, rep, ex)
+    a.close()
+    b.close()

@@ -303,3 +303,52 @@ def test_tuning_cache_persists_across_processes(tmp_path):
     n2, c2, t2 = map(int, second.stdout.split()[-3:])
     assert (n2, c2, t2) == (0, c1, t1)
     assert len((tmp_path / "tuning.jsonl").read_text().splitlines()) == 1
+
+
+@pytest.fixture(scope="module")
+def c3_subset():
+    """Four simulations of the batched uneven configuration, kept in their order there:
+    the one with the most pair work per step (12 molecules, 2,157 residues, a 387-residue
+    chain, 15 replicas), the one with the longest chain (400 residues), a 12-molecule one
+    with 8 replicas and the one with the least pair work (2 molecules, 172 residues)."""
+    wl = workloads.make("c3")
+    sizes = [sum(m.n for m in s.molecules) ** 2 - sum(m.n ** 2 for m in s.molecules) for s in wl.sims]
+    most = int(np.argmax(sizes))
+    least = int(np.argmin(sizes))
+    longest = max(range(len(wl.sims)), key=lambda i: max(m.n for m in wl.sims[i].molecules))
+    eight = next(i for i, s in enumerate(wl.sims) if len(s.temperatures) == 8 and len(s.molecules) == 12)
+    ids = sorted({most, least, longest, eight})
+    assert len(ids) == 4
+    return wl, ids
+
+
+def test_batched_uneven_subset_matches_oracle(c3_subset):
+    wl, ids = c3_subset
+    sims = [wl.sims[i] for i in ids]
+    e = engine_for(wl, sims, cluster=1, threads=512)
+    assert e.launch_shape()[2]  # resident, as in the full configuration
+    # initial molecule-pair matrices of the first and last replica of every simulation
+    for s, sim in enumerate(sims):
+        xyz = np.concatenate([m.xyz for m in sim.molecules]).astype(np.float32)
+        ref = oracle_matrix(wl, sim, xyz)
+        scale = np.abs(ref).max()
+        for r in (0, len(sim.temperatures) - 1):
+            E, _ = e.matrix(s, r)
+            assert np.all(np.abs(E - ref) <= REL * np.abs(ref) + 1e-7 * scale), (ids[s], r, np.abs(E - ref).max())
+    # two exchange blocks, every simulation against its own oracle run (same Philox
+    # streams: the engine numbers replicas across simulations in the order added)
+    blocks, steps = 2, 30
+    e.run(blocks, steps, exchange_after_last=True)
+    assert e.error_bits() == 0
+    off = 0
+    for s, sim in enumerate(sims):
+        o = OracleRemc(sim.molecules, wl.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
+                       sim.move_weights, sim.rigid_rotate_prob, None, None, seed=wl.seed, rep_off=off, sim_index=s)
+        orep, oex = o.run(blocks, steps, exchange_after_last=True, threads=o.R)
+        compare_runs(e, o, sim_index=s)
+        for b in range(blocks):
+            er, ex = e.report(s, b)
+            assert np.allclose(er, orep[b], equal_nan=True), (ids[s], b)
+            assert tuple(ex) == tuple(oex[b]), (ids[s], b)
+        off += o.R
+    e.close()

@@ -3,8 +3,10 @@
 Hosts that run inside another framework's device-memory pool, under a fixed memory
 budget, or in a loop that must not allocate, call this variant instead of
 CUDA_EonDevice; it uses a static device array as scratch.  Its result must equal
-CUDA_EonDevice's on the same inputs, call after call.  This file is collected last
-so that a failure here leaves every other test already run; it also passes alone.
+CUDA_EonDevice's on the same inputs, call after call, and both must be within 1e-5 of
+the FP64 oracle.  The largest accepted size (16384 residues: 128 tiles, 8256 CTAs)
+fills the static array exactly; one residue more is refused.  This file is collected
+last so that a failure here leaves every other test already run; it also passes alone.
 """
 import ctypes
 
@@ -40,6 +42,7 @@ def L(refdata):
 
 
 def energies(L, pos, meta, box):
+    """CUDA_EonDevice once, then CUDA_EonDevice_noalloc twice in a row."""
     L.CUDA_setBoxDimension(box)
     dp, dm = device_array(pos), device_array(meta)
     out = []
@@ -51,35 +54,54 @@ def energies(L, pos, meta, box):
     return out
 
 
+def check_all(L, refdata, pos, meta, box):
+    lib_ref, first, second = energies(L, pos, meta, box)
+    e64 = oracle.E_packed(oracle.FP64, pos, meta, refdata["lj_table"], box)[2]
+    for v in (lib_ref, first, second):
+        assert abs(v - e64) <= REL * abs(e64) + 1e-12, (v, e64)
+    assert abs(first - lib_ref) <= REL * abs(lib_ref) + 1e-12
+    assert abs(second - lib_ref) <= REL * abs(lib_ref) + 1e-12
+
+
 def test_noalloc_matches_cuda_eondevice_twice(L, refdata):
     for i in (1, 3, 8):
         mols = oracle.build_replica(["conf%d/1a" % i, "conf%d/1b" % i], refdata, 1000.0)
         pos, meta = oracle.pack_replica(mols, 32)
-        ref, first, second = energies(L, pos, meta, 1000.0)
-        assert abs(first - ref) <= REL * abs(ref) + 1e-12
-        assert abs(second - ref) <= REL * abs(ref) + 1e-12
+        check_all(L, refdata, pos, meta, 1000.0)
 
 
-def test_noalloc_large_system_and_limit(L, refdata):
-    rng = np.random.default_rng(7)
-    n = 6000
-    P = -(-n // 32) * 32
+def lattice_packed(n, P, seed, spacing=6.5):
+    """n residues in rigid domains of 300 residues on a jittered cubic lattice (no
+    clashes, so the sum is not dominated by a few huge repulsive terms), padded to P with
+    the reference's padding records.  Returns pos, meta and the periodic box edge."""
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(n ** (1.0 / 3.0)))
+    box = side * spacing
+    g = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
     pos = np.zeros((P, 4), np.float32)
     meta = np.zeros((P, 4), np.float32)
-    pos[:n, :3] = rng.uniform(0, 200.0, (n, 3))
+    pos[:n, :3] = g * spacing + rng.uniform(-0.6, 0.6, (n, 3))
     pos[:n, 3] = 1.0 + np.arange(n) // 300          # rigid domain per 300 residues
     meta[:n] = np.stack([rng.integers(0, 20, n), rng.choice([-1.0, 0.0, 1.0], n), rng.uniform(4.5, 7, n),
                          np.arange(n) // 300 + 0.25], 1)
     pos[n:, 3] = -2.0
     meta[n:, 0] = 20.0
-    ref, first, second = energies(L, pos, meta, 200.0)
-    assert abs(first - ref) <= REL * abs(ref) + 1e-12
-    assert abs(second - ref) <= REL * abs(ref) + 1e-12
-    # above the static scratch's limit the call is refused, not run
-    big = np.zeros((16416, 4), np.float32)
-    res = ctypes.c_double(3.0)
-    L.CUDA_EonDevice_noalloc(None, None, None, None, None, None, ctypes.byref(res), 32, 16416, 0)
-    assert res.value == 0.0
-    with pytest.raises(cgppd_gb300.CgppdError):
-        cgppd_gb300.check("over the limit")
-    del big
+    return pos, meta, float(box)
+
+
+def test_noalloc_large_system(L, refdata):
+    pos, meta, box = lattice_packed(6000, 6016, 7)
+    check_all(L, refdata, pos, meta, box)
+
+
+def test_noalloc_at_the_limit_and_above(L, refdata):
+    # 16384 residues: 128 tiles of 128, 8256 CTAs -- every CTA slot of the static array
+    pos, meta, box = lattice_packed(16384, 16384, 11)
+    check_all(L, refdata, pos, meta, box)
+    # one residue more is refused before anything is launched (no device memory is read)
+    for size in (16385, 16416):
+        res = ctypes.c_double(3.0)
+        L.CUDA_EonDevice_noalloc(None, None, None, None, None, None, ctypes.byref(res), 32, size, 0)
+        assert res.value == 0.0
+        with pytest.raises(cgppd_gb300.CgppdError):
+            cgppd_gb300.check("over the limit")
