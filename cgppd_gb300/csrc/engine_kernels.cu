@@ -50,8 +50,14 @@ namespace cg = cooperative_groups;
 namespace cgppd {
 
 constexpr int kTableStride = 32;
+// Contact table entry of a type pair in shared memory: (-4 Eij in kcal/mol, the s6
+// threshold of the repulsive branch: 1/2 where Eij > 0, +inf otherwise).
+constexpr int kTableBytes = kTableStride * kTableStride * (int)sizeof(float2);
 constexpr int kMaxThreads = 512;
 constexpr int kMaxWarps = kMaxThreads / 32;
+// Slack (A) on top of two bounding radii before a molecule pair skips the per-pair
+// minimum image: covers the float rounding of positions, centres and rotations.
+constexpr float kImageMargin = 0.05f;
 
 struct MoveDesc {
     int m, start, n, type, kind;
@@ -70,8 +76,9 @@ struct MoveDesc {
 struct SmemLayout {
     int table, mols, ipos, irel, iexcl, idisp, iq, ipq, iqq, ej, rowp, row;  // always
     int rcv;                                                         // clusters: pushed partial rows
+    int shift, rad;                                                  // per-molecule image shifts, radii
     int lst[12];                                                     // resident + flexible: static lists
-    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM, QP;                    // resident only
+    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM, QP, RMOL;              // resident only
     int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
     int total;
 };
@@ -118,7 +125,7 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
 {
     SmemLayout L;
     int off = 0;
-    L.table = off;  off += kTableStride * kTableStride * 4;
+    L.table = off;  off += kTableBytes;
     L.mols = off;   off = align16(off + (int)sizeof(DevMol) * max_m);
     L.ipos = off;   off += 16 * max_mol;
     L.irel = off;   off += 16 * max_mol;
@@ -132,7 +139,9 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     L.row = off;    off = align16(off + 8 * (max_m + 1));
     // [2 step parities][C source ranks][max_m + 1] (last entry: internal energy)
     L.rcv = off;    off = align16(off + (C > 1 ? 2 * C * (max_m + 1) * 8 : 0));
-    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = L.QP = 0;
+    L.shift = off;  off += 16 * max_m;
+    L.rad = off;    off = align16(off + 4 * max_m);
+    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = L.QP = L.RMOL = 0;
     if (resident) {
         L.P = off;      off += 16 * max_n;
         L.Q = off;      off += 16 * max_n;
@@ -143,6 +152,7 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
         L.INTRA = off;  off = align16(off + 8 * max_m);
         L.ROWSUM = off; off = align16(off + 8 * max_m);
         L.QP = off;     off = align16(off + 2 * max_n);  // charged-first positions
+        L.RMOL = off;   off = align16(off + 2 * max_n);  // molecule of each residue
     }
     for (int k = 0; k < 12; ++k)
         L.lst[k] = 0;
@@ -356,30 +366,74 @@ __device__ __forceinline__ float3 normalized(float x, float y, float z)
 }
 
 
-// Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with
-// (q*sqrt(DHF), type) in qa/qb.  `table` holds -4 Eij (kcal/mol): the LJ term is
+__device__ __forceinline__ void load_table(float2 *s_table, const float *table, int t, int T)
+{
+    for (int k = t; k < kTableStride * kTableStride; k += T) {
+        const float v = table[k];
+        s_table[k] = make_float2(v, v < 0.0f ? 0.5f : __int_as_float(0x7f800000));
+    }
+}
+
+// Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with the
+// charge q*sqrt(DHF) of a in qa.x and its type in qa.y (int bits), b's charge in qb and
+// `col` the table column of b's type (col[type_a * kTableStride]).  The LJ term is
 // u = (-4 Eij) s6 (s6 - 1), and 2 Eij - u on the repulsive branch (Eij > 0, s6 > 1/2),
 // the same values as lj_term with one multiplication less (power-of-two scaling).
-template <bool DH = true>
-__device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float *table, float L,
+// MI = false skips the minimum image: the caller has already moved b to the periodic
+// image that every pair of the two molecules takes (see the per-step molecule shifts in
+// k_mc), so a - b is the minimum-image difference itself.
+template <bool DH, bool MI>
+__device__ __forceinline__ float pair_term(float4 a, float2 qa, float4 b, float qb, const float2 *col, float L,
                                            float invL)
 {
-    const float dx = min_image(a.x - b.x, L, invL);
-    const float dy = min_image(a.y - b.y, L, invL);
-    const float dz = min_image(a.z - b.z, L, invL);
+    const float dx = MI ? min_image(a.x - b.x, L, invL) : a.x - b.x;
+    const float dy = MI ? min_image(a.y - b.y, L, invL) : a.y - b.y;
+    const float dz = MI ? min_image(a.z - b.z, L, invL) : a.z - b.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float inv_r = rsqrt_sfu(r2);
-    const float r = r2 * inv_r;
-    const float m4e = table[__float_as_int(qa.y) * kTableStride + __float_as_int(qb.y)];
+    const float2 e = col[__float_as_int(qa.y) * kTableStride];
     const float so = (a.w + b.w) * inv_r;  // sigma_ij / r
     const float s2 = so * so;
     const float s6 = s2 * s2 * s2;
-    float u = m4e * s6 * (s6 - 1.0f);
-    if (m4e < 0.0f && s6 > 0.5f)
-        u = fmaf(-0.5f, m4e, -u);
+    float u = e.x * fmaf(s6, s6, -s6);
+    if (s6 > e.y)
+        u = fmaf(-0.5f, e.x, -u);
     if (!DH)  // one of the pair uncharged: no Debye-Hueckel term
         return u;
-    return u + qa.x * qb.x * ex2_sfu(r * (-kLog2e / kXi)) * inv_r;
+    return u + qa.x * qb * ex2_sfu(r2 * inv_r * (-kLog2e / kXi)) * inv_r;
+}
+
+template <bool DH = true>
+__device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float2 *table, float L,
+                                           float invL)
+{
+    return pair_term<DH, true>(a, qa, b, qb.x, table + __float_as_int(qb.y), L, invL);
+}
+
+// Pair terms of residues i = i0, i0 + g, ... < i1 of the mover (records ipv / iqv) with
+// one residue b of another molecule: four independent partial sums, folded into the
+// float-float accumulator every 32 terms.  Returns the first index of the sequence at or
+// past i1 (where the next span of the same sequence starts).
+template <bool DH, bool MI>
+__device__ __forceinline__ int pair_span(const float4 *ipv, const float2 *iqv, int i0, int i1, int g, float4 b,
+                                          float qb, const float2 *col, float L, float invL, FF &acc, float &p0,
+                                          float &p1, float &p2, float &p3)
+{
+    int i = i0, cntp = 0;
+    for (; i + 3 * g < i1; i += 4 * g) {
+        p0 += pair_term<DH, MI>(ipv[i], iqv[i], b, qb, col, L, invL);
+        p1 += pair_term<DH, MI>(ipv[i + g], iqv[i + g], b, qb, col, L, invL);
+        p2 += pair_term<DH, MI>(ipv[i + 2 * g], iqv[i + 2 * g], b, qb, col, L, invL);
+        p3 += pair_term<DH, MI>(ipv[i + 3 * g], iqv[i + 3 * g], b, qb, col, L, invL);
+        if (++cntp == 8) {
+            ff_add(acc, (p0 + p1) + (p2 + p3));
+            p0 = p1 = p2 = p3 = 0.f;
+            cntp = 0;
+        }
+    }
+    for (; i < i1; i += g)
+        p0 += pair_term<DH, MI>(ipv[i], iqv[i], b, qb, col, L, invL);
+    return i;
 }
 
 // Repulsive crowder pair in kcal/mol, the reference's REPULSIVE_CROWDING build
@@ -509,7 +563,8 @@ __device__ void bonded_delta(const Lists &a, const DevMol &mol, const float4 *pn
 // subtraction, bonded terms) of a molecule at the state's positions, by one CTA; the
 // same value in every thread.
 __device__ FF intra_full_cta(const Lists &Ls, const DevMol &mol, const float4 *P, const float4 *Q,
-                             const unsigned char *TY, const int4 *EX, const float *table, float L, float invL, FF *red)
+                             const unsigned char *TY, const int4 *EX, const float2 *table, float L, float invL,
+                             FF *red)
 {
     const int t = threadIdx.x, T = blockDim.x, warp = t >> 5, lane = t & 31, NW = T >> 5;
     const int n = mol.count, st = mol.start;
@@ -1010,7 +1065,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible, DA ? 1 : 0, C, a.lmax);
     // screening is on for this simulation (uniform over the cluster: one simulation)
     const bool da_on = DA && a.sim_da[s] != 0;
-    float *s_table = reinterpret_cast<float *>(smem + Ly.table);
+    float2 *s_table = reinterpret_cast<float2 *>(smem + Ly.table);
     DevMol *s_mols = reinterpret_cast<DevMol *>(smem + Ly.mols);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
     float4 *s_irel = reinterpret_cast<float4 *>(smem + Ly.irel);
@@ -1020,6 +1075,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     float4 *s_ipq = reinterpret_cast<float4 *>(smem + Ly.ipq);
     float2 *s_iqq = reinterpret_cast<float2 *>(smem + Ly.iqq);
     unsigned short *s_qpos = reinterpret_cast<unsigned short *>(smem + Ly.QP);
+    unsigned short *s_rmol = reinterpret_cast<unsigned short *>(smem + Ly.RMOL);
+    float4 *s_shift = reinterpret_cast<float4 *>(smem + Ly.shift);
+    float *s_rad = reinterpret_cast<float *>(smem + Ly.rad);
     float2 *s_ej = reinterpret_cast<float2 *>(smem + Ly.ej);
     FF *s_rowp = reinterpret_cast<FF *>(smem + Ly.rowp);
     FF *s_row = reinterpret_cast<FF *>(smem + Ly.row);
@@ -1049,8 +1107,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     FF *INTRAf = reinterpret_cast<FF *>(smem + Ly.INTRA);
     FF *ROWSUMf = reinterpret_cast<FF *>(smem + Ly.ROWSUM);
 
-    for (int k = t; k < kTableStride * kTableStride; k += T)
-        s_table[k] = a.table[k];
+    load_table(s_table, a.table, t, T);
     for (int k = t; k < M; k += T) {
         DevMol mk = a.mols[S.mol_off + k];
         mk.pair_lanes = pair_lanes(mk.count, N, C, NW);
@@ -1064,6 +1121,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             sP[i] = make_float4(p.x, p.y, p.z, sr.x);
             sQ[i] = make_float4(q.x, q.y, q.z, sr.y);
             sTY[i] = (unsigned char)__float_as_int(sr.z);
+            s_rmol[i] = (unsigned short)__float_as_int(sr.w);
             if (QF)
                 s_qpos[i] = a.rqpos[S.res_off + i];
         }
@@ -1080,6 +1138,21 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             EMf[k] = ff_from(__ldcg(&gE[k]));
         __syncthreads();
     }
+    // bounding radius of every rigid molecule about its centre (rotations keep it up to
+    // float rounding); flexible molecules change shape and get none
+    for (int k = t; k < M; k += T)
+        s_rad[k] = 0.0f;
+    __syncthreads();
+    for (int i = t; i < N; i += T) {
+        const float4 q = RES ? Q[i] : __ldcg(&gQ[i]);
+        const int mi = RES ? (int)s_rmol[i] : __float_as_int(gST[i].w);
+        const float d = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
+        atomicMax(reinterpret_cast<int *>(&s_rad[mi]), __float_as_int(d));
+    }
+    __syncthreads();
+    for (int k = t; k < M; k += T)
+        if (s_mols[k].flags & kMolFlexible)
+            s_rad[k] = __int_as_float(0x7f800000);
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
     const float tstep = a.tstep[g];
     const float rstep = (float)a.rstep[g];
@@ -1315,6 +1388,30 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 s_iqq[k] = make_float2(sr.y, sr.z);
             }
         }
+        // The periodic image of every other molecule k for this proposal.  Where the
+        // centres' minimum-image separation plus both bounding radii stays below half a box
+        // on every axis, every residue pair of the mover and k takes the image of the two
+        // centres, so the pair loop shifts k's residues once (by the box times the rounded
+        // centre separation) instead of taking the minimum image of every pair: the same
+        // periodic image as the per-pair rule (src/CudaFunctions.cu:321-333), exactly so
+        // where the shift is zero.  Flexible molecules and unclear cases keep the per-pair
+        // rule (w = 0); without a periodic box there is nothing to take (w = 1, no shift).
+        for (int k = t; k < M; k += T) {
+            float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (L == 0.0f) {
+                sh.w = 1.0f;
+            } else if (!flexmol && k != m) {
+                const float4 ck = ld_state<RES>(&CEN[k]);
+                const float lim = 0.5f * L - (s_rad[m] + s_rad[k] + kImageMargin);
+                const float dx = mv.wcx - ck.x, dy = mv.wcy - ck.y, dz = mv.wcz - ck.z;
+                const float kx = __fadd_rn(__fmaf_rn(dx, invL, 12582912.0f), -12582912.0f);
+                const float ky = __fadd_rn(__fmaf_rn(dy, invL, 12582912.0f), -12582912.0f);
+                const float kz = __fadd_rn(__fmaf_rn(dz, invL, 12582912.0f), -12582912.0f);
+                if (fabsf(fmaf(-L, kx, dx)) < lim && fabsf(fmaf(-L, ky, dy)) < lim && fabsf(fmaf(-L, kz, dz)) < lim)
+                    sh = make_float4(L * kx, L * ky, L * kz, 1.0f);
+            }
+            s_shift[k] = sh;
+        }
         __syncthreads();
         if (type == kFlex && !nullm) {
             // rotate the branch about the pivot, accumulate the displacement
@@ -1427,38 +1524,32 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 }
                 ff_add(acc, p0);
             } else if (valid) {
-                const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
-                const float2 qj = make_float2(sj.y, sj.z);
+                const int j = (o < start) ? o : o + n;
+                const int mj = RES ? (int)s_rmol[j] : __float_as_int(sj.w);
+                const float4 sh = s_shift[mj];
+                const float qj = sj.y;
+                const float2 *col = s_table + __float_as_int(sj.z);
                 // four independent partial sums (instruction-level parallelism), folded
                 // into the float-float accumulator every 32 terms
                 float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-                int i = sub, cntp = 0;
-                for (; i + 3 * g < nqm; i += 4 * g) {
-                    p0 += pair_kcal(ipv[i], iqv[i], rj, qj, s_table, L, invL);
-                    p1 += pair_kcal(ipv[i + g], iqv[i + g], rj, qj, s_table, L, invL);
-                    p2 += pair_kcal(ipv[i + 2 * g], iqv[i + 2 * g], rj, qj, s_table, L, invL);
-                    p3 += pair_kcal(ipv[i + 3 * g], iqv[i + 3 * g], rj, qj, s_table, L, invL);
-                    if (++cntp == 8) {
-                        ff_add(acc, (p0 + p1) + (p2 + p3));
-                        p0 = p1 = p2 = p3 = 0.f;
-                        cntp = 0;
-                    }
+                if (sh.w != 0.0f) {
+                    // one periodic image for the whole molecule pair: no per-pair minimum image
+                    const float4 rj = make_float4(pj.x + sh.x, pj.y + sh.y, pj.z + sh.z, RES ? pj.w : sj.x);
+                    const int i2 = pair_span<true, false>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1, p2,
+                                                         p3);
+                    ff_add(acc, (p0 + p1) + (p2 + p3));
+                    p0 = p1 = p2 = p3 = 0.f;
+                    pair_span<false, false>(ipv, iqv, i2, n, g, rj, qj, col, L, invL,
+                                            acc, p0, p1, p2, p3);
+                } else {
+                    const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
+                    const int i2 = pair_span<true, true>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1, p2,
+                                                         p3);
+                    ff_add(acc, (p0 + p1) + (p2 + p3));
+                    p0 = p1 = p2 = p3 = 0.f;
+                    pair_span<false, true>(ipv, iqv, i2, n, g, rj, qj, col, L, invL,
+                                           acc, p0, p1, p2, p3);
                 }
-                for (; i < nqm; i += g)
-                    p0 += pair_kcal(ipv[i], iqv[i], rj, qj, s_table, L, invL);
-                for (; i + 3 * g < n; i += 4 * g) {
-                    p0 += pair_kcal<false>(ipv[i], iqv[i], rj, qj, s_table, L, invL);
-                    p1 += pair_kcal<false>(ipv[i + g], iqv[i + g], rj, qj, s_table, L, invL);
-                    p2 += pair_kcal<false>(ipv[i + 2 * g], iqv[i + 2 * g], rj, qj, s_table, L, invL);
-                    p3 += pair_kcal<false>(ipv[i + 3 * g], iqv[i + 3 * g], rj, qj, s_table, L, invL);
-                    if (++cntp == 8) {
-                        ff_add(acc, (p0 + p1) + (p2 + p3));
-                        p0 = p1 = p2 = p3 = 0.f;
-                        cntp = 0;
-                    }
-                }
-                for (; i < n; i += g)
-                    p0 += pair_kcal<false>(ipv[i], iqv[i], rj, qj, s_table, L, invL);
                 ff_add(acc, (p0 + p1) + (p2 + p3));
             }
             // segmented tree sum towards the group's first lane: after the step with offset
@@ -1839,12 +1930,11 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
         return;
     const int r = g - S.rep_off, N = S.N, M = S.M;
     const SmemLayout Ly = smem_layout(a.max_mol, a.max_n, a.max_m, a.max_n, 0, a.any_flexible);
-    float *s_table = reinterpret_cast<float *>(smem + Ly.table);
+    float2 *s_table = reinterpret_cast<float2 *>(smem + Ly.table);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
     float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
     int4 *s_iexcl = reinterpret_cast<int4 *>(smem + Ly.iexcl);
-    for (int k = t; k < kTableStride * kTableStride; k += T)
-        s_table[k] = a.table[k];
+    load_table(s_table, a.table, t, T);
     const DevMol mol = a.mols[S.mol_off + am];
     const long long st0 = S.state_off + (long long)r * N;
     const float4 *stat = a.rstat + S.res_off;
@@ -2080,12 +2170,11 @@ __global__ void __launch_bounds__(128) k_pose_samples(EngineArgs a, const int4 *
     const float4 *Q = a.rel + st0, *P = a.pos + st0;
     const float4 *CEN = a.center + S.molst_off + (long long)r * M;
     const float4 *stat = a.rstat + S.res_off;
-    float *s_table = reinterpret_cast<float *>(smem);
-    float4 *s_pa = reinterpret_cast<float4 *>(smem + kTableStride * kTableStride * 4);
-    float2 *s_qa = reinterpret_cast<float2 *>(smem + kTableStride * kTableStride * 4 + 16 * a.max_mol);
+    float2 *s_table = reinterpret_cast<float2 *>(smem);
+    float4 *s_pa = reinterpret_cast<float4 *>(smem + kTableBytes);
+    float2 *s_qa = reinterpret_cast<float2 *>(smem + kTableBytes + 16 * a.max_mol);
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
-    for (int k = t; k < kTableStride * kTableStride; k += T)
-        s_table[k] = a.table[k];
+    load_table(s_table, a.table, t, T);
     if (t == 0) {
         const float4 c = CEN[ma];
         float R[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
@@ -2151,7 +2240,7 @@ __global__ void __launch_bounds__(128) k_pose_samples(EngineArgs a, const int4 *
 cudaError_t launch_pose_samples(const EngineArgs &a, const int4 *items, int n, uint32_t key0, uint32_t key1, float *X,
                                 float *Y, cudaStream_t stream)
 {
-    const size_t smem = (size_t)kTableStride * kTableStride * 4 + 24 * (size_t)a.max_mol;
+    const size_t smem = (size_t)kTableBytes + 24 * (size_t)a.max_mol;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_pose_samples, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)

@@ -345,7 +345,11 @@ def test_batched_uneven_subset_matches_oracle(c3_subset):
         o = OracleRemc(sim.molecules, wl.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
                        sim.move_weights, sim.rigid_rotate_prob, None, None, seed=wl.seed, rep_off=off, sim_index=s)
         orep, oex = o.run(blocks, steps, exchange_after_last=True, threads=o.R)
-        compare_runs(e, o, sim_index=s)
+        # the engine rotates in float, the reference loop in double: the coordinates of
+        # the two runs differ by that rounding, and near contact the energies of the two
+        # coordinate sets differ by up to ~1e-5 relative; each engine total is still held
+        # to 1e-5 of the FP64 energy of its own coordinates
+        compare_runs(e, o, sim_index=s, traj_rel=1e-4)
         for b in range(blocks):
             er, ex = e.report(s, b)
             assert np.allclose(er, orep[b], equal_nan=True), (ids[s], b)
