@@ -50,9 +50,9 @@ namespace cg = cooperative_groups;
 namespace cgppd {
 
 constexpr int kTableStride = 32;
-// Contact table entry of a type pair in shared memory: (-4 Eij in kcal/mol, the s6
-// threshold of the repulsive branch: 1/2 where Eij > 0, +inf otherwise).
-constexpr int kTableBytes = kTableStride * kTableStride * (int)sizeof(float2);
+// Contact table in shared memory: -4 Eij in kcal/mol per type pair (4 bytes: a warp's
+// lookups of one row fall in one 128-byte line).
+constexpr int kTableBytes = kTableStride * kTableStride * (int)sizeof(float);
 constexpr int kMaxThreads = 512;
 constexpr int kMaxWarps = kMaxThreads / 32;
 // Slack (A) on top of two bounding radii before a molecule pair skips the per-pair
@@ -93,21 +93,23 @@ __host__ __device__ inline int da_rows(int max_m) { return (((max_m - 1 > 1 ? ma
 
 __host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
 
-// Lanes per other residue j in the inter-pair loop of a move of an n-residue molecule
-// (N residues in the simulation, C CTAs of W warps): g lanes share one j and take every
-// g-th residue i of the mover, a warp holds floor(32 / g) such groups.  Cost of the busiest
-// thread: passes over the CTA's slice x (ceil(n / g) pairs + a per-j overhead for the
-// loads and the log2(g)-step reduction); the cheapest g wins, ties to the smaller g.
+// Lanes per group in the inter-pair loop of a move of an n-residue molecule (N residues
+// in the simulation, C CTAs of W warps): a group of g lanes takes two other residues j
+// per pass (each mover residue record read from shared memory serves two pair terms)
+// and each of its lanes every g-th residue i of the mover; a warp holds floor(32 / g)
+// groups.  Cost of the busiest thread: passes over the CTA's slice x (2 ceil(n / g)
+// pairs + a per-pass overhead for the loads and the log2(g)-step reductions); the
+// cheapest g wins, ties to the smaller g.
 __host__ __device__ inline int pair_lanes(int n, int N, int C, int W) {
     const int sl = (N - n + C - 1) / C;
     int best = 1, best_cost = 0x7fffffff;
     for (int g = 1; g <= 32 && g <= (n > 1 ? n : 1); ++g) {
-        const int per = W * (32 / g);
+        const int per = 2 * W * (32 / g);
         const int passes = (sl + per - 1) / per;
         int lg = 0;
         while ((1 << lg) < g)
             ++lg;
-        const int cost = passes * ((n + g - 1) / g + 2 + lg);
+        const int cost = passes * (2 * ((n + g - 1) / g) + 4 + 2 * lg);
         if (cost < best_cost) {
             best_cost = cost;
             best = g;
@@ -366,12 +368,10 @@ __device__ __forceinline__ float3 normalized(float x, float y, float z)
 }
 
 
-__device__ __forceinline__ void load_table(float2 *s_table, const float *table, int t, int T)
+__device__ __forceinline__ void load_table(float *s_table, const float *table, int t, int T)
 {
-    for (int k = t; k < kTableStride * kTableStride; k += T) {
-        const float v = table[k];
-        s_table[k] = make_float2(v, v < 0.0f ? 0.5f : __int_as_float(0x7f800000));
-    }
+    for (int k = t; k < kTableStride * kTableStride; k += T)
+        s_table[k] = table[k];
 }
 
 // Pair energy in kcal/mol of residue records a (position, sigma/2) and b, with the
@@ -383,7 +383,7 @@ __device__ __forceinline__ void load_table(float2 *s_table, const float *table, 
 // image that every pair of the two molecules takes (see the per-step molecule shifts in
 // k_mc), so a - b is the minimum-image difference itself.
 template <bool DH, bool MI>
-__device__ __forceinline__ float pair_term(float4 a, float2 qa, float4 b, float qb, const float2 *col, float L,
+__device__ __forceinline__ float pair_term(float4 a, float2 qa, float4 b, float qb, const float *col, float L,
                                            float invL)
 {
     const float dx = MI ? min_image(a.x - b.x, L, invL) : a.x - b.x;
@@ -391,20 +391,20 @@ __device__ __forceinline__ float pair_term(float4 a, float2 qa, float4 b, float 
     const float dz = MI ? min_image(a.z - b.z, L, invL) : a.z - b.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float inv_r = rsqrt_sfu(r2);
-    const float2 e = col[__float_as_int(qa.y) * kTableStride];
+    const float m4e = col[__float_as_int(qa.y) * kTableStride];
     const float so = (a.w + b.w) * inv_r;  // sigma_ij / r
     const float s2 = so * so;
     const float s6 = s2 * s2 * s2;
-    float u = e.x * fmaf(s6, s6, -s6);
-    if (s6 > e.y)
-        u = fmaf(-0.5f, e.x, -u);
+    float u = m4e * fmaf(s6, s6, -s6);
+    if (m4e < 0.0f && s6 > 0.5f)
+        u = fmaf(-0.5f, m4e, -u);
     if (!DH)  // one of the pair uncharged: no Debye-Hueckel term
         return u;
     return u + qa.x * qb * ex2_sfu(r2 * inv_r * (-kLog2e / kXi)) * inv_r;
 }
 
 template <bool DH = true>
-__device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float2 *table, float L,
+__device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float *table, float L,
                                            float invL)
 {
     return pair_term<DH, true>(a, qa, b, qb.x, table + __float_as_int(qb.y), L, invL);
@@ -416,7 +416,7 @@ __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2
 // past i1 (where the next span of the same sequence starts).
 template <bool DH, bool MI>
 __device__ __forceinline__ int pair_span(const float4 *ipv, const float2 *iqv, int i0, int i1, int g, float4 b,
-                                          float qb, const float2 *col, float L, float invL, FF &acc, float &p0,
+                                          float qb, const float *col, float L, float invL, FF &acc, float &p0,
                                           float &p1, float &p2, float &p3)
 {
     int i = i0, cntp = 0;
@@ -433,6 +433,41 @@ __device__ __forceinline__ int pair_span(const float4 *ipv, const float2 *iqv, i
     }
     for (; i < i1; i += g)
         p0 += pair_term<DH, MI>(ipv[i], iqv[i], b, qb, col, L, invL);
+    return i;
+}
+
+// Pair terms of residues i = i0, i0 + g, ... < i1 of the mover with two residues ba and
+// bb of other molecules: each mover record is loaded once for both, two i per iteration
+// (four independent partial sums), folded into the float-float accumulators every 32
+// terms per residue.  Returns the first index of the sequence at or past i1.
+template <bool DH, bool MI>
+__device__ __forceinline__ int pair_span2(const float4 *ipv, const float2 *iqv, int i0, int i1, int g, float4 ba,
+                                           float qba, const float *cola, float4 bb, float qbb, const float *colb,
+                                           float L, float invL, FF &acca, FF &accb, float &a0, float &a1, float &b0,
+                                           float &b1)
+{
+    int i = i0, cnt = 0;
+    for (; i + g < i1; i += 2 * g) {
+        const float4 r0 = ipv[i], r1 = ipv[i + g];
+        const float2 q0 = iqv[i], q1 = iqv[i + g];
+        a0 += pair_term<DH, MI>(r0, q0, ba, qba, cola, L, invL);
+        b0 += pair_term<DH, MI>(r0, q0, bb, qbb, colb, L, invL);
+        a1 += pair_term<DH, MI>(r1, q1, ba, qba, cola, L, invL);
+        b1 += pair_term<DH, MI>(r1, q1, bb, qbb, colb, L, invL);
+        if (++cnt == 16) {
+            ff_add(acca, a0 + a1);
+            ff_add(accb, b0 + b1);
+            a0 = a1 = b0 = b1 = 0.f;
+            cnt = 0;
+        }
+    }
+    if (i < i1) {
+        const float4 r0 = ipv[i];
+        const float2 q0 = iqv[i];
+        a0 += pair_term<DH, MI>(r0, q0, ba, qba, cola, L, invL);
+        b0 += pair_term<DH, MI>(r0, q0, bb, qbb, colb, L, invL);
+        i += g;
+    }
     return i;
 }
 
@@ -563,7 +598,7 @@ __device__ void bonded_delta(const Lists &a, const DevMol &mol, const float4 *pn
 // subtraction, bonded terms) of a molecule at the state's positions, by one CTA; the
 // same value in every thread.
 __device__ FF intra_full_cta(const Lists &Ls, const DevMol &mol, const float4 *P, const float4 *Q,
-                             const unsigned char *TY, const int4 *EX, const float2 *table, float L, float invL,
+                             const unsigned char *TY, const int4 *EX, const float *table, float L, float invL,
                              FF *red)
 {
     const int t = threadIdx.x, T = blockDim.x, warp = t >> 5, lane = t & 31, NW = T >> 5;
@@ -1065,7 +1100,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         smem_layout(a.max_mol, slice, a.max_m, a.max_n, RES ? 1 : 0, a.any_flexible, DA ? 1 : 0, C, a.lmax);
     // screening is on for this simulation (uniform over the cluster: one simulation)
     const bool da_on = DA && a.sim_da[s] != 0;
-    float2 *s_table = reinterpret_cast<float2 *>(smem + Ly.table);
+    float *s_table = reinterpret_cast<float *>(smem + Ly.table);
     DevMol *s_mols = reinterpret_cast<DevMol *>(smem + Ly.mols);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
     float4 *s_irel = reinterpret_cast<float4 *>(smem + Ly.irel);
@@ -1474,8 +1509,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int sl = (nother + C - 1) / C;
         const int o0 = rank * sl, o1 = min(nother, o0 + sl);
         const int cnt = max(0, o1 - o0);
-        // g lanes per j (each takes every g-th i), floor(32 / g) groups of lanes per warp;
-        // the lanes past the last whole group idle
+        // groups of g lanes take two j per pass (each lane every g-th i), floor(32 / g)
+        // groups per warp; the lanes past the last whole group idle
         const int g = s_mols[m].pair_lanes, jw = 32 / g;
         // a rigid mover is read in charged-first order: its first nqm residues take the
         // full pair term, the rest the Lennard-Jones part alone (no charge, no Debye-Hueckel)
@@ -1490,28 +1525,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int sub = lane % g, grp = lane / g;
         const int jl = warp * jw + grp, jstride = NW * jw;
         const bool lane_on = grp < jw;
-        // residue record of this thread's next j, loaded one iteration ahead
-        float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
+        auto jof = [&](int o) { return (o < start) ? o : o + n; };
         auto stat_of = [&](int j) -> float4 {
             return RES ? make_float4(0.f, Q[j].w, __int_as_float((int)TY[j]), 0.f) : ST[j];
         };
-        if (lane_on && jl < cnt) {
-            const int o = o0 + jl, j = (o < start) ? o : o + n;
-            npj = ld_state<RES>(&P[j]);
-            nsj = stat_of(j);
-        }
-        for (int base = 0; base < cnt; base += jstride) {
-            const int o = o0 + base + jl;
-            const bool valid = lane_on && (base + jl) < cnt;
-            const bool crowd = mcrowd || ((o < start) ? o : o + n) >= cstart;
-            const float4 pj = npj, sj = nsj;
-            if (lane_on && base + jstride + jl < cnt) {
-                const int on = o + jstride, jn = (on < start) ? on : on + n;
-                npj = ld_state<RES>(&P[jn]);
-                nsj = stat_of(jn);
-            }
-            FF acc{0.f, 0.f};
-            if (valid && crowd) {
+        // one pair of the mover's residue sequence with one other residue (the crowder
+        // branch, and the general per-pair minimum image), into acc
+        auto one_j = [&](int j, float4 pj, float4 sj, FF &acc) {
+            if (mcrowd || j >= cstart) {
                 float p0 = 0.f;
                 int cntp = 0;
                 for (int i = sub; i < n; i += g) {
@@ -1523,44 +1544,94 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     }
                 }
                 ff_add(acc, p0);
-            } else if (valid) {
-                const int j = (o < start) ? o : o + n;
-                const int mj = RES ? (int)s_rmol[j] : __float_as_int(sj.w);
-                const float4 sh = s_shift[mj];
-                const float qj = sj.y;
-                const float2 *col = s_table + __float_as_int(sj.z);
-                // four independent partial sums (instruction-level parallelism), folded
-                // into the float-float accumulator every 32 terms
-                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-                if (sh.w != 0.0f) {
-                    // one periodic image for the whole molecule pair: no per-pair minimum image
-                    const float4 rj = make_float4(pj.x + sh.x, pj.y + sh.y, pj.z + sh.z, RES ? pj.w : sj.x);
-                    const int i2 = pair_span<true, false>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1, p2,
-                                                         p3);
-                    ff_add(acc, (p0 + p1) + (p2 + p3));
-                    p0 = p1 = p2 = p3 = 0.f;
-                    pair_span<false, false>(ipv, iqv, i2, n, g, rj, qj, col, L, invL,
-                                            acc, p0, p1, p2, p3);
+                return;
+            }
+            const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
+            const float *col = s_table + __float_as_int(sj.z);
+            float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+            const int i2 = pair_span<true, true>(ipv, iqv, sub, nqm, g, rj, sj.y, col, L, invL, acc, p0, p1, p2, p3);
+            ff_add(acc, (p0 + p1) + (p2 + p3));
+            p0 = p1 = p2 = p3 = 0.f;
+            pair_span<false, true>(ipv, iqv, i2, n, g, rj, sj.y, col, L, invL, acc, p0, p1, p2, p3);
+            ff_add(acc, (p0 + p1) + (p2 + p3));
+        };
+        // residue records of this group's next two j, loaded one pass ahead
+        float4 npa = make_float4(0.f, 0.f, 0.f, 0.f), nsa = npa, npb = npa, nsb = npa;
+        if (lane_on && jl < cnt) {
+            npa = ld_state<RES>(&P[jof(o0 + jl)]);
+            nsa = stat_of(jof(o0 + jl));
+        }
+        if (lane_on && jstride + jl < cnt) {
+            npb = ld_state<RES>(&P[jof(o0 + jstride + jl)]);
+            nsb = stat_of(jof(o0 + jstride + jl));
+        }
+        for (int base = 0; base < cnt; base += 2 * jstride) {
+            const int oa = o0 + base + jl, ob = oa + jstride;
+            const bool va = lane_on && (base + jl) < cnt, vb = lane_on && (base + jstride + jl) < cnt;
+            const float4 pa = npa, sa = nsa, pb = npb, sb = nsb;
+            if (lane_on && base + 2 * jstride + jl < cnt) {
+                npa = ld_state<RES>(&P[jof(oa + 2 * jstride)]);
+                nsa = stat_of(jof(oa + 2 * jstride));
+            }
+            if (lane_on && base + 3 * jstride + jl < cnt) {
+                npb = ld_state<RES>(&P[jof(ob + 2 * jstride)]);
+                nsb = stat_of(jof(ob + 2 * jstride));
+            }
+            FF acca{0.f, 0.f}, accb{0.f, 0.f};
+            if (va) {
+                const int ja = jof(oa), jb = vb ? jof(ob) : ja;
+                const float4 pbb = vb ? pb : pa, sbb = vb ? sb : sa;
+                const bool crowd = mcrowd || ja >= cstart || jb >= cstart;
+                const float4 sha = s_shift[RES ? (int)s_rmol[ja] : __float_as_int(sa.w)];
+                const float4 shb = s_shift[RES ? (int)s_rmol[jb] : __float_as_int(sbb.w)];
+                if (crowd) {
+                    one_j(ja, pa, sa, acca);
+                    if (vb)
+                        one_j(jb, pb, sb, accb);
                 } else {
-                    const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
-                    const int i2 = pair_span<true, true>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1, p2,
-                                                         p3);
-                    ff_add(acc, (p0 + p1) + (p2 + p3));
-                    p0 = p1 = p2 = p3 = 0.f;
-                    pair_span<false, true>(ipv, iqv, i2, n, g, rj, qj, col, L, invL,
-                                           acc, p0, p1, p2, p3);
+                    const float *cola = s_table + __float_as_int(sa.z), *colb = s_table + __float_as_int(sbb.z);
+                    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+                    if (sha.w != 0.0f && shb.w != 0.0f) {
+                        // one periodic image per molecule pair: no per-pair minimum image
+                        const float4 ra = make_float4(pa.x + sha.x, pa.y + sha.y, pa.z + sha.z, RES ? pa.w : sa.x);
+                        const float4 rb = make_float4(pbb.x + shb.x, pbb.y + shb.y, pbb.z + shb.z,
+                                                      RES ? pbb.w : sbb.x);
+                        const int i2 = pair_span2<true, false>(ipv, iqv, sub, nqm, g, ra, sa.y, cola, rb, sbb.y,
+                                                               colb, L, invL, acca, accb, a0, a1, b0, b1);
+                        ff_add(acca, a0 + a1);
+                        ff_add(accb, b0 + b1);
+                        a0 = a1 = b0 = b1 = 0.f;
+                        pair_span2<false, false>(ipv, iqv, i2, n, g, ra, sa.y, cola, rb, sbb.y, colb, L, invL,
+                                                 acca, accb, a0, a1, b0, b1);
+                    } else {
+                        const float4 ra = make_float4(pa.x, pa.y, pa.z, RES ? pa.w : sa.x);
+                        const float4 rb = make_float4(pbb.x, pbb.y, pbb.z, RES ? pbb.w : sbb.x);
+                        const int i2 = pair_span2<true, true>(ipv, iqv, sub, nqm, g, ra, sa.y, cola, rb, sbb.y,
+                                                              colb, L, invL, acca, accb, a0, a1, b0, b1);
+                        ff_add(acca, a0 + a1);
+                        ff_add(accb, b0 + b1);
+                        a0 = a1 = b0 = b1 = 0.f;
+                        pair_span2<false, true>(ipv, iqv, i2, n, g, ra, sa.y, cola, rb, sbb.y, colb, L, invL,
+                                                acca, accb, a0, a1, b0, b1);
+                    }
+                    ff_add(acca, a0 + a1);
+                    ff_add(accb, b0 + b1);
                 }
-                ff_add(acc, (p0 + p1) + (p2 + p3));
             }
-            // segmented tree sum towards the group's first lane: after the step with offset
-            // d, lane sub holds the lanes [sub, min(sub + 2d, g)) of its group
+            // segmented tree sums towards the group's first lane: after the step with
+            // offset d, lane sub holds the lanes [sub, min(sub + 2d, g)) of its group
             for (int d = 1; d < g; d <<= 1) {
-                const FF w{__shfl_down_sync(0xffffffffu, acc.hi, d), __shfl_down_sync(0xffffffffu, acc.lo, d)};
-                if (sub + d < g)
-                    ff_add_ff(acc, w);
+                const FF wa{__shfl_down_sync(0xffffffffu, acca.hi, d), __shfl_down_sync(0xffffffffu, acca.lo, d)};
+                const FF wb{__shfl_down_sync(0xffffffffu, accb.hi, d), __shfl_down_sync(0xffffffffu, accb.lo, d)};
+                if (sub + d < g) {
+                    ff_add_ff(acca, wa);
+                    ff_add_ff(accb, wb);
+                }
             }
-            if (valid && sub == 0)
-                s_ej[o - o0] = make_float2(acc.hi, acc.lo);
+            if (va && sub == 0)
+                s_ej[oa - o0] = make_float2(acca.hi, acca.lo);
+            if (vb && sub == 0)
+                s_ej[ob - o0] = make_float2(accb.hi, accb.lo);
         }
 
         // ---- internal energy of a flexible molecule (intra pairs split over the cluster).
@@ -1930,7 +2001,7 @@ __global__ void __launch_bounds__(256) k_init_rows(EngineArgs a)
         return;
     const int r = g - S.rep_off, N = S.N, M = S.M;
     const SmemLayout Ly = smem_layout(a.max_mol, a.max_n, a.max_m, a.max_n, 0, a.any_flexible);
-    float2 *s_table = reinterpret_cast<float2 *>(smem + Ly.table);
+    float *s_table = reinterpret_cast<float *>(smem + Ly.table);
     float4 *s_ipos = reinterpret_cast<float4 *>(smem + Ly.ipos);
     float2 *s_iq = reinterpret_cast<float2 *>(smem + Ly.iq);
     int4 *s_iexcl = reinterpret_cast<int4 *>(smem + Ly.iexcl);
@@ -2170,7 +2241,7 @@ __global__ void __launch_bounds__(128) k_pose_samples(EngineArgs a, const int4 *
     const float4 *Q = a.rel + st0, *P = a.pos + st0;
     const float4 *CEN = a.center + S.molst_off + (long long)r * M;
     const float4 *stat = a.rstat + S.res_off;
-    float2 *s_table = reinterpret_cast<float2 *>(smem);
+    float *s_table = reinterpret_cast<float *>(smem);
     float4 *s_pa = reinterpret_cast<float4 *>(smem + kTableBytes);
     float2 *s_qa = reinterpret_cast<float2 *>(smem + kTableBytes + 16 * a.max_mol);
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;

@@ -1,13 +1,20 @@
-"""Build oracle/_ref/libcgppd_ref.so from the reference's own energy sources.
+"""Build the reference's own code as a checker, from the reference tree (read-only).
 
-TEST INFRASTRUCTURE ONLY.  Compiles, in place from the reference tree (read-only),
-the translation units of the energy layer that need no external library --
-src/{Potential,Residue,AminoAcids,AminoAcid,Geometry,Quaternion,vector3f,
-TorsionalLookupMatrix}.cpp -- with the reference's own flags for the flexible-linker
-CPU build (-O2 -std=c++11 -DEnableFlexibleLinkers, Makefile:5 and :60-62), plus
-oracle/ref_harness.cpp.  Output goes only to oracle/_ref/ (git-ignored).  The MC layer
-(Molecule, Replica, Simulation) needs GSL and logog, which are not installed here, so
-it is not built.
+TEST INFRASTRUCTURE ONLY.  Output goes only to oracle/_ref/ (git-ignored):
+
+* oracle/_ref/libcgppd_ref.so -- the energy layer, src/{Potential,Residue,AminoAcids,
+  AminoAcid,Geometry,Quaternion,vector3f,TorsionalLookupMatrix}.cpp, with
+  oracle/ref_harness.cpp;
+* oracle/_ref/cgppd_ref_mc -- the MC layer as well (src/Molecule.cpp, Replica.cpp,
+  Simulation.cpp, unmodified), driven by oracle/ref_mc_harness.cpp; two vector
+  operators without a return statement are routed to oracle/ref_fixups.cpp at link time.  GSL and logog are
+  not installed here: oracle/ref_stubs/ declares the calls the reference makes, and
+  oracle/ref_rng.cpp answers its random-number calls with the GB300 engine's Philox
+  draws (the Philox itself from oracle/cgppd_oracle.c); logging is compiled out.
+
+Both use the reference's own flags for the flexible-linker CPU build (-O2 -std=c++11
+-DEnableFlexibleLinkers, Makefile:5 and :60-62) plus -ffp-contract=off, so that an
+aarch64 host rounds like the x86-64 build the reference was run on.
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
 
@@ -23,6 +30,8 @@ OUT_DIR = os.path.join(HERE, "_ref")
 OUT = os.path.join(OUT_DIR, "libcgppd_ref.so")
 UNITS = ["Potential", "Residue", "AminoAcids", "AminoAcid", "Geometry", "Quaternion", "vector3f",
          "TorsionalLookupMatrix"]
+MC_UNITS = UNITS + ["Molecule", "Replica", "Simulation"]
+MC_OUT = os.path.join(OUT_DIR, "cgppd_ref_mc")
 
 
 def reference_root():
@@ -54,5 +63,39 @@ def build(ref_root=None):
     return OUT
 
 
+def build_mc(ref_root=None):
+    """oracle/_ref/cgppd_ref_mc: the reference's MC layer with the Philox-protocol
+    generators, or None without the reference tree."""
+    ref_root = ref_root or reference_root()
+    if ref_root is None:
+        return None
+    src = os.path.join(ref_root, "src")
+    if not os.path.isdir(src):
+        return None
+    os.makedirs(OUT_DIR, exist_ok=True)
+    stubs = os.path.join(HERE, "ref_stubs")
+    cpp = [os.path.join(src, u + ".cpp") for u in MC_UNITS] + [os.path.join(HERE, f) for f in
+                                                                ("ref_rng.cpp", "ref_fixups.cpp",
+                                                                 "ref_mc_harness.cpp")]
+    philox = os.path.join(HERE, "cgppd_oracle.c")
+    deps = cpp + [philox, __file__] + [os.path.join(dp, f) for dp, _, fs in os.walk(stubs) for f in fs]
+    if os.path.exists(MC_OUT) and all(os.path.getmtime(d) < os.path.getmtime(MC_OUT) for d in deps):
+        return MC_OUT
+    obj = os.path.join(OUT_DIR, "philox.o")
+    steps = [["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-c", philox, "-o", obj],
+             ["g++", "-O2", "-std=c++11", "-ffp-contract=off", "-w", "-DEnableFlexibleLinkers",
+              '-DHGVERSION="cgppd reference (checker build)"', "-I" + stubs, "-I" + src, "-o", MC_OUT] + cpp +
+             [obj, "-lpthread", "-lm",
+              # src/vector3f.cpp:105-117 lack a return statement: calls go to ref_fixups.cpp
+              "-Wl,--wrap=_ZN8Vector3fpLES_", "-Wl,--wrap=_ZN8Vector3fmIES_"]]
+    for cmd in steps:
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference MC layer failed to build:\n" + r.stdout[-4000:])
+    return MC_OUT
+
+
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else None))
+    root = sys.argv[1] if len(sys.argv) > 1 else None
+    print(build(root))
+    print(build_mc(root))

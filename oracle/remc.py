@@ -83,7 +83,10 @@ class OracleRemc:
     def __init__(self, molecules, table, box, temperatures, translate_steps, rotate_steps, move_weights=(1, 1, 1, 1),
                  rigid_rotate_prob=0.5, torsion_V=None, torsion_phase=None, seed=20261203, mode=0,
                  sample_frequency=0, sample_after=0, bound_threshold=-1.1844, rep_off=0, sim_index=0,
-                 repulsive_crowding=False):
+                 repulsive_crowding=False, centers=None, rel=None):
+        """`centers` [M, 3] and `rel` [N, 3] give the molecules' centres and relative
+        positions where they are not the float mean of the coordinates and the
+        differences from it (a state loaded from the reference's own run)."""
         L = _declare()
         self.L = L
         self.keep = []
@@ -214,9 +217,11 @@ class OracleRemc:
         R = len(temperatures)
         self.R = R
         xyz = np.concatenate([np.asarray(m.xyz, np.float32) for m in molecules])
-        cen = np.stack([float_mean(m.xyz) for m in molecules]).astype(np.float32)
+        cen = np.stack([float_mean(m.xyz) for m in molecules]).astype(np.float32) if centers is None else \
+            np.ascontiguousarray(centers, np.float32).reshape(M, 3)
         rel = np.concatenate([(np.asarray(m.xyz, np.float32) - cen[k]).astype(np.float32)
-                              for k, m in enumerate(molecules)])
+                              for k, m in enumerate(molecules)]) if rel is None else \
+            np.ascontiguousarray(rel, np.float32).reshape(N, 3)
         self.pos = np.ascontiguousarray(np.broadcast_to(xyz, (R, N, 3)).copy())
         self.rel = np.ascontiguousarray(np.broadcast_to(rel, (R, N, 3)).copy())
         self.center = np.ascontiguousarray(np.broadcast_to(cen, (R, M, 3)).copy())

@@ -146,3 +146,22 @@ def device_array(arr):
 
 def ptr(t):
     return ctypes.c_void_p(t.data_ptr())
+
+
+REF_MC = os.path.join(ROOT, "tests", "golden", "ref_mc_trajectories.json")
+
+
+def ref_mc_config(name):
+    """One configuration of the reference trajectory fixtures (make_ref_mc_golden.py):
+    (config dict, molecules, centres [M,3], relative positions [N,3], per-replica
+    temperatures, translate steps, rotate steps)."""
+    import json
+    from oracle import ref_mc
+    with open(REF_MC) as f:
+        d = json.load(f)
+    cfg = d["configs"][name]
+    cfg["seed"], cfg["block"] = d["seed"], d["block"]
+    mols, cen, rel = ref_mc.system(cfg)
+    ini = ref_mc.replicas(cfg, "initial")
+    return cfg, mols, cen, rel, ini["temperature"], ini["translate_step"].astype(np.float32), \
+        ini["rotate_step"].astype(np.float64)
