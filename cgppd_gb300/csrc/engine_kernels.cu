@@ -76,9 +76,9 @@ struct MoveDesc {
 struct SmemLayout {
     int table, mols, ipos, irel, iexcl, idisp, iq, ipq, iqq, ej, rowp, row;  // always
     int rcv;                                                         // clusters: pushed partial rows
-    int shift, rad;                                                  // per-molecule image shifts, radii
+    int rad;                                                         // bounding radius per molecule
     int lst[12];                                                     // resident + flexible: static lists
-    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM, QP, RMOL;              // resident only
+    int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM, QP;                    // resident only
     int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
     int total;
 };
@@ -93,23 +93,22 @@ __host__ __device__ inline int da_rows(int max_m) { return (((max_m - 1 > 1 ? ma
 
 __host__ __device__ inline int align16(int v) { return (v + 15) & ~15; }
 
-// Lanes per group in the inter-pair loop of a move of an n-residue molecule (N residues
-// in the simulation, C CTAs of W warps): a group of g lanes takes two other residues j
-// per pass (each mover residue record read from shared memory serves two pair terms)
-// and each of its lanes every g-th residue i of the mover; a warp holds floor(32 / g)
-// groups.  Cost of the busiest thread: passes over the CTA's slice x (2 ceil(n / g)
-// pairs + a per-pass overhead for the loads and the log2(g)-step reductions); the
-// cheapest g wins, ties to the smaller g.
+// Lanes per other residue j in the inter-pair loop of a move of an n-residue molecule
+// (N residues in the simulation, C CTAs of W warps): g lanes share one j and take every
+// g-th residue i of the mover, a warp holds floor(32 / g) such groups.  Cost of the busiest
+// thread: passes over the CTA's slice x (ceil(n / g) pairs + a per-j overhead for the
+// loads, the periodic image and the log2(g)-step reduction); the cheapest g wins, ties
+// to the smaller g.
 __host__ __device__ inline int pair_lanes(int n, int N, int C, int W) {
     const int sl = (N - n + C - 1) / C;
     int best = 1, best_cost = 0x7fffffff;
     for (int g = 1; g <= 32 && g <= (n > 1 ? n : 1); ++g) {
-        const int per = 2 * W * (32 / g);
+        const int per = W * (32 / g);
         const int passes = (sl + per - 1) / per;
         int lg = 0;
         while ((1 << lg) < g)
             ++lg;
-        const int cost = passes * (2 * ((n + g - 1) / g) + 4 + 2 * lg);
+        const int cost = passes * ((n + g - 1) / g + 2 + lg);
         if (cost < best_cost) {
             best_cost = cost;
             best = g;
@@ -141,9 +140,8 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     L.row = off;    off = align16(off + 8 * (max_m + 1));
     // [2 step parities][C source ranks][max_m + 1] (last entry: internal energy)
     L.rcv = off;    off = align16(off + (C > 1 ? 2 * C * (max_m + 1) * 8 : 0));
-    L.shift = off;  off += 16 * max_m;
     L.rad = off;    off = align16(off + 4 * max_m);
-    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = L.QP = L.RMOL = 0;
+    L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = L.QP = 0;
     if (resident) {
         L.P = off;      off += 16 * max_n;
         L.Q = off;      off += 16 * max_n;
@@ -154,7 +152,6 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
         L.INTRA = off;  off = align16(off + 8 * max_m);
         L.ROWSUM = off; off = align16(off + 8 * max_m);
         L.QP = off;     off = align16(off + 2 * max_n);  // charged-first positions
-        L.RMOL = off;   off = align16(off + 2 * max_n);  // molecule of each residue
     }
     for (int k = 0; k < 12; ++k)
         L.lst[k] = 0;
@@ -433,41 +430,6 @@ __device__ __forceinline__ int pair_span(const float4 *ipv, const float2 *iqv, i
     }
     for (; i < i1; i += g)
         p0 += pair_term<DH, MI>(ipv[i], iqv[i], b, qb, col, L, invL);
-    return i;
-}
-
-// Pair terms of residues i = i0, i0 + g, ... < i1 of the mover with two residues ba and
-// bb of other molecules: each mover record is loaded once for both, two i per iteration
-// (four independent partial sums), folded into the float-float accumulators every 32
-// terms per residue.  Returns the first index of the sequence at or past i1.
-template <bool DH, bool MI>
-__device__ __forceinline__ int pair_span2(const float4 *ipv, const float2 *iqv, int i0, int i1, int g, float4 ba,
-                                           float qba, const float *cola, float4 bb, float qbb, const float *colb,
-                                           float L, float invL, FF &acca, FF &accb, float &a0, float &a1, float &b0,
-                                           float &b1)
-{
-    int i = i0, cnt = 0;
-    for (; i + g < i1; i += 2 * g) {
-        const float4 r0 = ipv[i], r1 = ipv[i + g];
-        const float2 q0 = iqv[i], q1 = iqv[i + g];
-        a0 += pair_term<DH, MI>(r0, q0, ba, qba, cola, L, invL);
-        b0 += pair_term<DH, MI>(r0, q0, bb, qbb, colb, L, invL);
-        a1 += pair_term<DH, MI>(r1, q1, ba, qba, cola, L, invL);
-        b1 += pair_term<DH, MI>(r1, q1, bb, qbb, colb, L, invL);
-        if (++cnt == 16) {
-            ff_add(acca, a0 + a1);
-            ff_add(accb, b0 + b1);
-            a0 = a1 = b0 = b1 = 0.f;
-            cnt = 0;
-        }
-    }
-    if (i < i1) {
-        const float4 r0 = ipv[i];
-        const float2 q0 = iqv[i];
-        a0 += pair_term<DH, MI>(r0, q0, ba, qba, cola, L, invL);
-        b0 += pair_term<DH, MI>(r0, q0, bb, qbb, colb, L, invL);
-        i += g;
-    }
     return i;
 }
 
@@ -1110,8 +1072,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     float4 *s_ipq = reinterpret_cast<float4 *>(smem + Ly.ipq);
     float2 *s_iqq = reinterpret_cast<float2 *>(smem + Ly.iqq);
     unsigned short *s_qpos = reinterpret_cast<unsigned short *>(smem + Ly.QP);
-    unsigned short *s_rmol = reinterpret_cast<unsigned short *>(smem + Ly.RMOL);
-    float4 *s_shift = reinterpret_cast<float4 *>(smem + Ly.shift);
     float *s_rad = reinterpret_cast<float *>(smem + Ly.rad);
     float2 *s_ej = reinterpret_cast<float2 *>(smem + Ly.ej);
     FF *s_rowp = reinterpret_cast<FF *>(smem + Ly.rowp);
@@ -1156,7 +1116,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             sP[i] = make_float4(p.x, p.y, p.z, sr.x);
             sQ[i] = make_float4(q.x, q.y, q.z, sr.y);
             sTY[i] = (unsigned char)__float_as_int(sr.z);
-            s_rmol[i] = (unsigned short)__float_as_int(sr.w);
             if (QF)
                 s_qpos[i] = a.rqpos[S.res_off + i];
         }
@@ -1174,20 +1133,24 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         __syncthreads();
     }
     // bounding radius of every rigid molecule about its centre (rotations keep it up to
-    // float rounding); flexible molecules change shape and get none
-    for (int k = t; k < M; k += T)
-        s_rad[k] = 0.0f;
+    // float rounding, which kImageMargin covers); flexible molecules change shape and get
+    // none.  One warp per molecule, after every thread has stored its DevMol records (the
+    // resident load above ends with a barrier; the global-state path has none).
     __syncthreads();
-    for (int i = t; i < N; i += T) {
-        const float4 q = RES ? Q[i] : __ldcg(&gQ[i]);
-        const int mi = RES ? (int)s_rmol[i] : __float_as_int(gST[i].w);
-        const float d = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
-        atomicMax(reinterpret_cast<int *>(&s_rad[mi]), __float_as_int(d));
+    for (int k = warp; k < M; k += NW) {
+        const DevMol &mk = s_mols[k];
+        float rmax = 0.0f;
+        for (int i = lane; i < mk.count; i += 32) {
+            const float4 q = RES ? Q[mk.start + i] : __ldcg(&gQ[mk.start + i]);
+            rmax = fmaxf(rmax, sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z))));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        if (lane == 0)
+            s_rad[k] = (mk.flags & kMolFlexible) ? __int_as_float(0x7f800000) : rmax;
     }
     __syncthreads();
-    for (int k = t; k < M; k += T)
-        if (s_mols[k].flags & kMolFlexible)
-            s_rad[k] = __int_as_float(0x7f800000);
     const float L = S.box, invL = (S.box != 0.0f) ? 1.0f / S.box : 0.0f;
     const float tstep = a.tstep[g];
     const float rstep = (float)a.rstep[g];
@@ -1423,30 +1386,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 s_iqq[k] = make_float2(sr.y, sr.z);
             }
         }
-        // The periodic image of every other molecule k for this proposal.  Where the
-        // centres' minimum-image separation plus both bounding radii stays below half a box
-        // on every axis, every residue pair of the mover and k takes the image of the two
-        // centres, so the pair loop shifts k's residues once (by the box times the rounded
-        // centre separation) instead of taking the minimum image of every pair: the same
-        // periodic image as the per-pair rule (src/CudaFunctions.cu:321-333), exactly so
-        // where the shift is zero.  Flexible molecules and unclear cases keep the per-pair
-        // rule (w = 0); without a periodic box there is nothing to take (w = 1, no shift).
-        for (int k = t; k < M; k += T) {
-            float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (L == 0.0f) {
-                sh.w = 1.0f;
-            } else if (!flexmol && k != m) {
-                const float4 ck = ld_state<RES>(&CEN[k]);
-                const float lim = 0.5f * L - (s_rad[m] + s_rad[k] + kImageMargin);
-                const float dx = mv.wcx - ck.x, dy = mv.wcy - ck.y, dz = mv.wcz - ck.z;
-                const float kx = __fadd_rn(__fmaf_rn(dx, invL, 12582912.0f), -12582912.0f);
-                const float ky = __fadd_rn(__fmaf_rn(dy, invL, 12582912.0f), -12582912.0f);
-                const float kz = __fadd_rn(__fmaf_rn(dz, invL, 12582912.0f), -12582912.0f);
-                if (fabsf(fmaf(-L, kx, dx)) < lim && fabsf(fmaf(-L, ky, dy)) < lim && fabsf(fmaf(-L, kz, dz)) < lim)
-                    sh = make_float4(L * kx, L * ky, L * kz, 1.0f);
-            }
-            s_shift[k] = sh;
-        }
         __syncthreads();
         if (type == kFlex && !nullm) {
             // rotate the branch about the pivot, accumulate the displacement
@@ -1509,8 +1448,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int sl = (nother + C - 1) / C;
         const int o0 = rank * sl, o1 = min(nother, o0 + sl);
         const int cnt = max(0, o1 - o0);
-        // groups of g lanes take two j per pass (each lane every g-th i), floor(32 / g)
-        // groups per warp; the lanes past the last whole group idle
+        // g lanes per j (each takes every g-th i), floor(32 / g) groups of lanes per warp;
+        // the lanes past the last whole group idle
         const int g = s_mols[m].pair_lanes, jw = 32 / g;
         // a rigid mover is read in charged-first order: its first nqm residues take the
         // full pair term, the rest the Lennard-Jones part alone (no charge, no Debye-Hueckel)
@@ -1525,14 +1464,47 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         const int sub = lane % g, grp = lane / g;
         const int jl = warp * jw + grp, jstride = NW * jw;
         const bool lane_on = grp < jw;
-        auto jof = [&](int o) { return (o < start) ? o : o + n; };
+        // Periodic images without a minimum image per pair: each other residue j is moved
+        // once to its image nearest the mover's centre.  Where that image lies more than
+        // the mover's bounding radius inside the half box around the centre on every
+        // axis, no mover residue is more than half a box from it, so the per-pair rule
+        // (src/CudaFunctions.cu:321-333) takes exactly that image for every pair and the
+        // loop takes the plain differences; warps with a j in the outer shell keep the
+        // per-pair minimum image.  (Flexible movers have no fixed radius: always the
+        // per-pair rule.)
+        const float hlim = (L != 0.0f && !flexmol) ? 0.5f * L - (s_rad[m] + kImageMargin) : -1.0f;
         auto stat_of = [&](int j) -> float4 {
             return RES ? make_float4(0.f, Q[j].w, __int_as_float((int)TY[j]), 0.f) : ST[j];
         };
-        // one pair of the mover's residue sequence with one other residue (the crowder
-        // branch, and the general per-pair minimum image), into acc
-        auto one_j = [&](int j, float4 pj, float4 sj, FF &acc) {
-            if (mcrowd || j >= cstart) {
+        // residue record of this thread's next j, loaded one iteration ahead
+        float4 npj = make_float4(0.f, 0.f, 0.f, 0.f), nsj = npj;
+        if (lane_on && jl < cnt) {
+            const int o = o0 + jl, j = (o < start) ? o : o + n;
+            npj = ld_state<RES>(&P[j]);
+            nsj = stat_of(j);
+        }
+        for (int base = 0; base < cnt; base += jstride) {
+            const int o = o0 + base + jl;
+            const bool valid = lane_on && (base + jl) < cnt;
+            const bool crowd = mcrowd || ((o < start) ? o : o + n) >= cstart;
+            const float4 pj = npj, sj = nsj;
+            if (lane_on && base + jstride + jl < cnt) {
+                const int on = o + jstride, jn = (on < start) ? on : on + n;
+                npj = ld_state<RES>(&P[jn]);
+                nsj = stat_of(jn);
+            }
+            // j's image nearest the mover's centre (the minimum-image rule applied once;
+            // exactly pj where that image is pj itself); the warp takes the loop without a
+            // per-pair minimum image when that image is inner for all of its j
+            const float kx = __fadd_rn(__fmaf_rn(pj.x - mv.wcx, invL, 12582912.0f), -12582912.0f);
+            const float ky = __fadd_rn(__fmaf_rn(pj.y - mv.wcy, invL, 12582912.0f), -12582912.0f);
+            const float kz = __fadd_rn(__fmaf_rn(pj.z - mv.wcz, invL, 12582912.0f), -12582912.0f);
+            const float bx = fmaf(-L, kx, pj.x), by = fmaf(-L, ky, pj.y), bz = fmaf(-L, kz, pj.z);
+            const bool inner = L == 0.0f || (fabsf(bx - mv.wcx) < hlim && fabsf(by - mv.wcy) < hlim &&
+                                             fabsf(bz - mv.wcz) < hlim);
+            const bool fast = __all_sync(0xffffffffu, inner || !valid || crowd);
+            FF acc{0.f, 0.f};
+            if (valid && crowd) {
                 float p0 = 0.f;
                 int cntp = 0;
                 for (int i = sub; i < n; i += g) {
@@ -1544,94 +1516,39 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     }
                 }
                 ff_add(acc, p0);
-                return;
-            }
-            const float4 rj = make_float4(pj.x, pj.y, pj.z, RES ? pj.w : sj.x);
-            const float *col = s_table + __float_as_int(sj.z);
-            float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-            const int i2 = pair_span<true, true>(ipv, iqv, sub, nqm, g, rj, sj.y, col, L, invL, acc, p0, p1, p2, p3);
-            ff_add(acc, (p0 + p1) + (p2 + p3));
-            p0 = p1 = p2 = p3 = 0.f;
-            pair_span<false, true>(ipv, iqv, i2, n, g, rj, sj.y, col, L, invL, acc, p0, p1, p2, p3);
-            ff_add(acc, (p0 + p1) + (p2 + p3));
-        };
-        // residue records of this group's next two j, loaded one pass ahead
-        float4 npa = make_float4(0.f, 0.f, 0.f, 0.f), nsa = npa, npb = npa, nsb = npa;
-        if (lane_on && jl < cnt) {
-            npa = ld_state<RES>(&P[jof(o0 + jl)]);
-            nsa = stat_of(jof(o0 + jl));
-        }
-        if (lane_on && jstride + jl < cnt) {
-            npb = ld_state<RES>(&P[jof(o0 + jstride + jl)]);
-            nsb = stat_of(jof(o0 + jstride + jl));
-        }
-        for (int base = 0; base < cnt; base += 2 * jstride) {
-            const int oa = o0 + base + jl, ob = oa + jstride;
-            const bool va = lane_on && (base + jl) < cnt, vb = lane_on && (base + jstride + jl) < cnt;
-            const float4 pa = npa, sa = nsa, pb = npb, sb = nsb;
-            if (lane_on && base + 2 * jstride + jl < cnt) {
-                npa = ld_state<RES>(&P[jof(oa + 2 * jstride)]);
-                nsa = stat_of(jof(oa + 2 * jstride));
-            }
-            if (lane_on && base + 3 * jstride + jl < cnt) {
-                npb = ld_state<RES>(&P[jof(ob + 2 * jstride)]);
-                nsb = stat_of(jof(ob + 2 * jstride));
-            }
-            FF acca{0.f, 0.f}, accb{0.f, 0.f};
-            if (va) {
-                const int ja = jof(oa), jb = vb ? jof(ob) : ja;
-                const float4 pbb = vb ? pb : pa, sbb = vb ? sb : sa;
-                const bool crowd = mcrowd || ja >= cstart || jb >= cstart;
-                const float4 sha = s_shift[RES ? (int)s_rmol[ja] : __float_as_int(sa.w)];
-                const float4 shb = s_shift[RES ? (int)s_rmol[jb] : __float_as_int(sbb.w)];
-                if (crowd) {
-                    one_j(ja, pa, sa, acca);
-                    if (vb)
-                        one_j(jb, pb, sb, accb);
+            } else if (valid) {
+                const float qj = sj.y;
+                const float *col = s_table + __float_as_int(sj.z);
+                const float sw = RES ? pj.w : sj.x;
+                // four independent partial sums (instruction-level parallelism), folded
+                // into the float-float accumulator every 32 terms
+                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+                if (fast) {
+                    const float4 rj = make_float4(bx, by, bz, sw);
+                    const int i2 = pair_span<true, false>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1,
+                                                          p2, p3);
+                    ff_add(acc, (p0 + p1) + (p2 + p3));
+                    p0 = p1 = p2 = p3 = 0.f;
+                    pair_span<false, false>(ipv, iqv, i2, n, g, rj, qj, col, L, invL, acc, p0, p1, p2, p3);
                 } else {
-                    const float *cola = s_table + __float_as_int(sa.z), *colb = s_table + __float_as_int(sbb.z);
-                    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
-                    if (sha.w != 0.0f && shb.w != 0.0f) {
-                        // one periodic image per molecule pair: no per-pair minimum image
-                        const float4 ra = make_float4(pa.x + sha.x, pa.y + sha.y, pa.z + sha.z, RES ? pa.w : sa.x);
-                        const float4 rb = make_float4(pbb.x + shb.x, pbb.y + shb.y, pbb.z + shb.z,
-                                                      RES ? pbb.w : sbb.x);
-                        const int i2 = pair_span2<true, false>(ipv, iqv, sub, nqm, g, ra, sa.y, cola, rb, sbb.y,
-                                                               colb, L, invL, acca, accb, a0, a1, b0, b1);
-                        ff_add(acca, a0 + a1);
-                        ff_add(accb, b0 + b1);
-                        a0 = a1 = b0 = b1 = 0.f;
-                        pair_span2<false, false>(ipv, iqv, i2, n, g, ra, sa.y, cola, rb, sbb.y, colb, L, invL,
-                                                 acca, accb, a0, a1, b0, b1);
-                    } else {
-                        const float4 ra = make_float4(pa.x, pa.y, pa.z, RES ? pa.w : sa.x);
-                        const float4 rb = make_float4(pbb.x, pbb.y, pbb.z, RES ? pbb.w : sbb.x);
-                        const int i2 = pair_span2<true, true>(ipv, iqv, sub, nqm, g, ra, sa.y, cola, rb, sbb.y,
-                                                              colb, L, invL, acca, accb, a0, a1, b0, b1);
-                        ff_add(acca, a0 + a1);
-                        ff_add(accb, b0 + b1);
-                        a0 = a1 = b0 = b1 = 0.f;
-                        pair_span2<false, true>(ipv, iqv, i2, n, g, ra, sa.y, cola, rb, sbb.y, colb, L, invL,
-                                                acca, accb, a0, a1, b0, b1);
-                    }
-                    ff_add(acca, a0 + a1);
-                    ff_add(accb, b0 + b1);
+                    const float4 rj = make_float4(pj.x, pj.y, pj.z, sw);
+                    const int i2 = pair_span<true, true>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1,
+                                                         p2, p3);
+                    ff_add(acc, (p0 + p1) + (p2 + p3));
+                    p0 = p1 = p2 = p3 = 0.f;
+                    pair_span<false, true>(ipv, iqv, i2, n, g, rj, qj, col, L, invL, acc, p0, p1, p2, p3);
                 }
+                ff_add(acc, (p0 + p1) + (p2 + p3));
             }
-            // segmented tree sums towards the group's first lane: after the step with
-            // offset d, lane sub holds the lanes [sub, min(sub + 2d, g)) of its group
+            // segmented tree sum towards the group's first lane: after the step with offset
+            // d, lane sub holds the lanes [sub, min(sub + 2d, g)) of its group
             for (int d = 1; d < g; d <<= 1) {
-                const FF wa{__shfl_down_sync(0xffffffffu, acca.hi, d), __shfl_down_sync(0xffffffffu, acca.lo, d)};
-                const FF wb{__shfl_down_sync(0xffffffffu, accb.hi, d), __shfl_down_sync(0xffffffffu, accb.lo, d)};
-                if (sub + d < g) {
-                    ff_add_ff(acca, wa);
-                    ff_add_ff(accb, wb);
-                }
+                const FF w{__shfl_down_sync(0xffffffffu, acc.hi, d), __shfl_down_sync(0xffffffffu, acc.lo, d)};
+                if (sub + d < g)
+                    ff_add_ff(acc, w);
             }
-            if (va && sub == 0)
-                s_ej[oa - o0] = make_float2(acca.hi, acca.lo);
-            if (vb && sub == 0)
-                s_ej[ob - o0] = make_float2(accb.hi, accb.lo);
+            if (valid && sub == 0)
+                s_ej[o - o0] = make_float2(acc.hi, acc.lo);
         }
 
         // ---- internal energy of a flexible molecule (intra pairs split over the cluster).
