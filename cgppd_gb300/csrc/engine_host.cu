@@ -169,6 +169,9 @@ struct cgppd_engine {
     DevBuf<float4> d_report;
     DevBuf<int2> d_exch_report;
     DevBuf<unsigned> d_errflags;
+    DevBuf<SampleRec> d_sample_log;  // boundconformations records (cgppd_engine_set_sample_log)
+    DevBuf<unsigned> d_sample_count;
+    int sample_cap = 0;
 
     std::vector<DevSim> h_sims;
     std::vector<DevMol> h_mols;
@@ -230,6 +233,9 @@ struct cgppd_engine {
         a.exch_report = d_exch_report.ptr;
         a.report_capacity = report_capacity;
         a.errflags = d_errflags.ptr;
+        a.sample_log = sample_cap > 0 ? d_sample_log.ptr : nullptr;
+        a.sample_count = d_sample_count.ptr;
+        a.sample_cap = sample_cap;
         a.seed_lo = (uint32_t)seed;
         a.seed_hi = (uint32_t)(seed >> 32);
         a.ntypes = ntypes;
@@ -739,6 +745,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     EngineArgs base = e->args();
     base.pos = pos.ptr, base.rel = rel.ptr, base.center = cen.ptr, base.emat = em.ptr, base.intra = in.ptr;
     base.potential = pot.ptr, base.stats = st.ptr, base.stepc = sc.ptr, base.pairc = pc.ptr, base.errflags = ef.ptr;
+    base.sample_log = nullptr;  // timing launches record no samples
     if (e->da)
         base.dastats = das.ptr;
     const int clusters[8] = {1, 2, 3, 4, 5, 6, 8, 16}, thread_opts[3] = {128, 256, 512};
@@ -1416,6 +1423,65 @@ int cgppd_engine_get_report(cgppd_engine *e, int sim, int row, float *per_temper
         rc |= cgppd_check(cudaMemcpy(exch2, e->d_exch_report.ptr + (long long)row * e->sims.size() + sim, sizeof(int2),
                                      cudaMemcpyDeviceToHost), "copy");
     return rc ? -1 : 0;
+}
+
+int cgppd_engine_set_sample_log(cgppd_engine *e, int per_replica)
+{
+    if (!e || !e->finalized || per_replica < 0)
+        return cgppd_fail("cgppd_engine_set_sample_log: engine not finalized or negative capacity");
+    if (cgppd_check(cudaDeviceSynchronize(), "sample log") != 0)
+        return -1;
+    e->sample_cap = 0;
+    e->d_sample_log.release();
+    if (per_replica > 0) {
+        if (e->d_sample_log.alloc((size_t)per_replica * e->total_replicas) != 0 ||
+            e->d_sample_count.zero((size_t)e->total_replicas) != 0)
+            return -1;
+        e->sample_cap = per_replica;
+    }
+    for (auto &kv : e->graphs)  // graphs captured the old arguments
+        cudaGraphExecDestroy(kv.second);
+    e->graphs.clear();
+    return 0;
+}
+
+int cgppd_engine_take_samples(cgppd_engine *e, int sim, int *counts, double *enc, double *potential,
+                              float *temperature, int *step)
+{
+    if (!e || sim < 0 || sim >= (int)e->h_sims.size())
+        return cgppd_fail("cgppd_engine_take_samples: bad simulation index");
+    const DevSim &S = e->h_sims[sim];
+    if (e->sample_cap <= 0) {
+        for (int r = 0; r < S.R; ++r)
+            counts[r] = 0;
+        return 0;
+    }
+    if (cgppd_check(cudaDeviceSynchronize(), "take samples") != 0)
+        return -1;
+    std::vector<unsigned> cnt(S.R);
+    std::vector<SampleRec> rec((size_t)S.R * e->sample_cap);
+    if (cgppd_check(cudaMemcpy(cnt.data(), e->d_sample_count.ptr + S.rep_off, sizeof(unsigned) * S.R,
+                               cudaMemcpyDeviceToHost), "take samples") != 0 ||
+        cgppd_check(cudaMemcpy(rec.data(), e->d_sample_log.ptr + (size_t)S.rep_off * e->sample_cap,
+                               sizeof(SampleRec) * rec.size(), cudaMemcpyDeviceToHost), "take samples") != 0 ||
+        cgppd_check(cudaMemset(e->d_sample_count.ptr + S.rep_off, 0, sizeof(unsigned) * S.R), "take samples") != 0)
+        return -1;
+    for (int r = 0; r < S.R; ++r) {
+        counts[r] = (int)cnt[r];
+        for (unsigned k = 0; k < cnt[r]; ++k) {
+            const SampleRec &x = rec[(size_t)r * e->sample_cap + k];
+            const size_t o = (size_t)r * e->sample_cap + k;
+            if (enc)
+                enc[o] = x.enc;
+            if (potential)
+                potential[o] = x.potential;
+            if (temperature)
+                temperature[o] = x.temperature;
+            if (step)
+                step[o] = x.step;
+        }
+    }
+    return 0;
 }
 
 int cgppd_engine_counters(cgppd_engine *e, unsigned long long *mc_steps, unsigned long long *pair_evals)

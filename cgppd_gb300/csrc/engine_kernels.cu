@@ -1860,6 +1860,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                     st.samplesSinceLastExchange++;
                     if ((float)e < S.bound_threshold)
                         st.boundSamples++;
+                    // the sample's line of boundconformations, when the host keeps them
+                    if (a.sample_log != nullptr && rank == 0) {
+                        const unsigned k = a.sample_count[g];
+                        if ((int)k < a.sample_cap) {
+                            a.sample_log[(long long)g * a.sample_cap + k] =
+                                SampleRec{e, ff_value(s_pot), temperature, (int)(mcstep + 1 - (unsigned)freq)};
+                            a.sample_count[g] = k + 1;
+                        } else {
+                            errbits |= 8u;  // log full: the sample is counted but not recorded
+                        }
+                    }
                 }
             }
         }

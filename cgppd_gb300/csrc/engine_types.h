@@ -91,6 +91,16 @@ struct ReplicaStats {
     int pad[3];
 };
 
+// One fraction-bound sample of a replica slot, the content of the line
+// Replica::sample writes to boundconformations (src/Replica.cpp:1037-1093): the
+// non-crowder inter-molecule energy, the replica's potential, the slot's temperature
+// and the first MC step of the sampling window.
+struct SampleRec {
+    double enc, potential;
+    float temperature;
+    int step;
+};
+
 struct EngineArgs {
     const DevSim *sims;
     const int *rep_sim;          // global replica -> simulation
@@ -132,6 +142,9 @@ struct EngineArgs {
     int2 *exch_report;           // per exchange: (exchanges, tests)
     int report_capacity;         // exchanges the report buffers hold per simulation
     unsigned *errflags;          // per replica error bits
+    SampleRec *sample_log;       // [total replicas][sample_cap] or null
+    unsigned *sample_count;      // records held per replica
+    int sample_cap;
     uint32_t seed_lo, seed_hi;
     int ntypes;
     int cluster;                 // CTAs per replica

@@ -11,7 +11,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <fstream>
+#include <tuple>
 #include <sstream>
 
 #include "../status.h"
@@ -475,6 +477,37 @@ void Simulation::exchange_frequency(int steps, int row)
     std::fprintf(exchangeFrequencyFile, "%10d %6.4f %6.4f\n", steps, acc, frac);
 }
 
+// The lines Replica::sample writes to boundconformations (src/Replica.cpp:1083-1091),
+// from the device's sample log: "step; E_nc (E); T" and the name of the sample's PDB
+// file, in the order one reference thread writes them (block, replica slot, step).  The
+// PDB files themselves are not written.
+void Simulation::write_samples(int steps_per_block, int cap)
+{
+    int R = 0;
+    cgppd_engine_sim_info(engine_, 0, nullptr, nullptr, &R);
+    std::vector<int> counts(R), step((size_t)R * cap);
+    std::vector<double> enc((size_t)R * cap), pot((size_t)R * cap);
+    std::vector<float> temp((size_t)R * cap);
+    if (cgppd_engine_take_samples(engine_, 0, counts.data(), enc.data(), pot.data(), temp.data(), step.data()) != 0)
+        throw "MC run failed.";
+    std::vector<std::tuple<int, int, int, size_t>> order;
+    for (int r = 0; r < R; ++r)
+        for (int k = 0; k < counts[r]; ++k) {
+            const size_t o = (size_t)r * cap + k;
+            order.emplace_back(step[o] / steps_per_block, r, step[o], o);
+        }
+    std::sort(order.begin(), order.end());
+    char name[512];
+    for (const auto &x : order) {
+        const size_t o = std::get<3>(x);
+        std::snprintf(name, sizeof(name), "%s/pdb/sample_%d_%0.1fK_%5.2f.pdb", outdir.c_str(), step[o],
+                      (double)temp[o], enc[o]);
+        std::fprintf(boundConformationsFile, "%d; %0.5f (%0.5f); %0.1f\n%s\n", step[o], enc[o], pot[o],
+                     (double)temp[o], name);
+    }
+    std::fflush(boundConformationsFile);
+}
+
 // Simulation::run (src/Simulation.cpp:709-873): REsteps blocks of MCsteps/REsteps MC
 // steps with REsteps-1 exchanges in between, all on the device; the per-exchange
 // reports are read back afterwards and written in the reference's formats.
@@ -486,8 +519,23 @@ void Simulation::run()
         return;
     const int K = parameters.MCsteps / parameters.REsteps;
     const int RE = parameters.REsteps;
-    if (cgppd_engine_run(engine_, RE, K, 0, nullptr) != 0)
-        throw "MC run failed.";
+    // the samples' lines of boundconformations come from the device's sample log, read
+    // back after chunks of blocks small enough for the log
+    const int freq = parameters.sampleFrequency;
+    const int per_block = freq > 0 ? (K + freq - 1) / freq : 0;
+    int chunk = RE;
+    if (per_block > 0) {
+        chunk = std::max(1, std::min(RE, 4096 / per_block));
+        if (cgppd_engine_set_sample_log(engine_, chunk * per_block) != 0)
+            throw "MC run failed.";
+    }
+    for (int b = 0; b < RE; b += chunk) {
+        const int nb = std::min(chunk, RE - b);
+        if (cgppd_engine_run(engine_, nb, K, (b + nb < RE) ? 1 : 0, nullptr) != 0)
+            throw "MC run failed.";
+        if (per_block > 0)
+            write_samples(K, chunk * per_block);
+    }
     if (cgppd_engine_final_report(engine_, RE - 1, nullptr) != 0 || cgppd_engine_synchronize(engine_) != 0)
         throw "MC run failed.";
     for (int steps = 1; steps < RE; ++steps) {

@@ -90,6 +90,7 @@ private:
     void closeSamplingFiles();
     void write_report_row(int mcsteps_label, int row);
     void exchange_frequency(int steps, int row);
+    void write_samples(int steps_per_block, int log_capacity);
 
     cgppd_engine *engine_ = nullptr;
     FILE *fractionBoundFile = nullptr, *boundConformationsFile = nullptr, *acceptanceRatioFile = nullptr,

@@ -48,6 +48,9 @@ _DECL = {
     "cgppd_engine_set_resident": (c_int, [c_void_p, c_int]),
     "cgppd_engine_checkpoint": (c_int, [c_void_p, ctypes.c_char_p]),
     "cgppd_engine_restore": (c_int, [c_void_p, ctypes.c_char_p]),
+    "cgppd_engine_set_sample_log": (c_int, [c_void_p, c_int]),
+    "cgppd_engine_take_samples": (c_int, [c_void_p, c_int, P(c_int), P(ctypes.c_double), P(ctypes.c_double),
+                                          P(c_float), P(c_int)]),
 }
 
 
@@ -241,6 +244,31 @@ class Engine:
 
     def last_launches(self):
         return _L().cgppd_engine_last_launches(self.h)
+
+    def set_sample_log(self, per_replica):
+        """Keep up to `per_replica` fraction-bound samples per replica on the device."""
+        self._sample_cap = int(per_replica)
+        _ok(_L().cgppd_engine_set_sample_log(self.h, int(per_replica)), "set_sample_log")
+
+    def take_samples(self, sim):
+        """The samples recorded since the last call, per replica slot: a list of record
+        arrays (step, non-crowder energy, potential, temperature), emptying the log."""
+        _, _, R = self.sim_info(sim)
+        cap = max(1, getattr(self, "_sample_cap", 0))
+        counts = np.zeros(R, np.int32)
+        enc = np.zeros(R * cap, np.float64)
+        pot = np.zeros(R * cap, np.float64)
+        temp = np.zeros(R * cap, np.float32)
+        step = np.zeros(R * cap, np.int32)
+        _ok(_L().cgppd_engine_take_samples(self.h, sim, _p(counts, c_int), _p(enc, ctypes.c_double),
+                                           _p(pot, ctypes.c_double), _p(temp, c_float), _p(step, c_int)),
+            "take_samples")
+        out = []
+        for r in range(R):
+            sl = slice(r * cap, r * cap + counts[r])
+            out.append({"step": step[sl].copy(), "enc": enc[sl].copy(), "potential": pot[sl].copy(),
+                        "temperature": temp[sl].copy()})
+        return out
 
     def checkpoint(self, path):
         _ok(_L().cgppd_engine_checkpoint(self.h, str(path).encode()), "checkpoint")

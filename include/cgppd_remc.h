@@ -149,13 +149,27 @@ int cgppd_engine_get_matrix(cgppd_engine *e, int sim, int replica, double *E, do
  * (exchanges, tests) of that exchange. */
 int cgppd_engine_get_report(cgppd_engine *e, int sim, int row, float *per_temperature4, int *exch2);
 
+/* Sample records for the reference's boundconformations file (src/Replica.cpp:1037-1093,
+ * which writes one line per fraction-bound sample: "step; E_nc (E); T").  After
+ * finalize, set_sample_log keeps up to `per_replica` samples per replica slot on the
+ * device (0 = none, the default); every sample taken while the log has room is
+ * recorded, a full log sets error bit 8.  take_samples copies one simulation's records
+ * and empties its logs: counts [n_replicas], and per slot r the records
+ * [r * per_replica, r * per_replica + counts[r]) of enc (non-crowder energy, kcal/mol),
+ * potential (kcal/mol), temperature (K) and step (first MC step of the sampling
+ * window), in the order they were taken.  Any record array may be NULL. */
+int cgppd_engine_set_sample_log(cgppd_engine *e, int per_replica);
+int cgppd_engine_take_samples(cgppd_engine *e, int sim, int *counts, double *enc, double *potential,
+                              float *temperature, int *step);
+
 /* MC steps done and residue-pair terms evaluated by all replicas since creation. */
 int cgppd_engine_counters(cgppd_engine *e, unsigned long long *mc_steps, unsigned long long *pair_evals);
 
 /* OR of the per-replica status bits: 1 a move type with no candidate residue was drawn
  * and left the molecule unchanged; 2 a proposal's energy change was not finite
  * (non-finite coordinates or energies) and the move was rejected; 4 an exchange test
- * met a non-finite potential and the pair did not exchange. */
+ * met a non-finite potential and the pair did not exchange; 8 a sample was taken while
+ * the sample log was full (see cgppd_engine_set_sample_log) and was not recorded. */
 unsigned cgppd_engine_error_bits(cgppd_engine *e);
 
 /* The same bits per replica of simulation `sim` (out: [n_replicas], replica-slot order). */

@@ -230,7 +230,18 @@ def remc_outputs(ref, arch):
         fvals = [[float(x) for x in ln.split(":", 1)[1].replace("|", " ").split()] for ln in frows]
         out["fraction_final_cumulative"] = fvals[-1][1::2]
         out["fileindex"] = text("fileindex").splitlines()
-        out["boundconformations_header"] = text("boundconformations").splitlines()[:2]
+        bc = text("boundconformations").splitlines()
+        out["boundconformations_header"] = bc[:2]
+        # per-temperature mean of the sampled replica potentials ("step; E_nc (E); T")
+        per_t = {}
+        for ln in bc[2:]:
+            if ";" not in ln:
+                continue
+            f = ln.split(";")
+            e = float(f[1].split("(")[1].split(")")[0])
+            per_t.setdefault(f[2].strip(), []).append(e)
+        out["sampled_energy_mean_by_temperature"] = {t: sum(v) / len(v) for t, v in per_t.items()}
+        out["sampled_energy_count_by_temperature"] = {t: len(v) for t, v in per_t.items()}
     return out
 
 

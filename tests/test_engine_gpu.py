@@ -356,3 +356,28 @@ def test_batched_uneven_subset_matches_oracle(c3_subset):
             assert tuple(ex) == tuple(oex[b]), (ids[s], b)
         off += o.R
     e.close()
+
+
+def test_sample_log_records_every_sample():
+    # fraction-bound samples every 10 steps: one record per sample and replica slot, in
+    # order, with the window's first step; a block-end sample holds the replica's
+    # potential and temperature at that point, and the non-crowder energy of a system
+    # of two rigid proteins is its total
+    wl = workloads.make("c0")
+    sim = subset(wl, 3)
+    e = engine_for(wl, [sim], sample_frequency=10, sample_after=0)
+    e.set_sample_log(25)
+    e.run(2, 100, exchange_after_last=False)
+    rec = e.take_samples(0)
+    rep = e.replicas(0)
+    for r in range(3):
+        assert list(rec[r]["step"]) == list(range(0, 200, 10))
+        assert rec[r]["potential"][-1] == pytest.approx(rep["potential"][r], rel=1e-12)
+        assert rec[r]["temperature"][-1] == rep["temperature"][r]
+        assert np.allclose(rec[r]["enc"], rec[r]["potential"], rtol=1e-12)
+    # the log was emptied; a full log records no more and says so (bit 8)
+    assert all(len(x["step"]) == 0 for x in e.take_samples(0))
+    e.run(3, 100, exchange_after_last=False)
+    assert all(len(x["step"]) == 25 for x in e.take_samples(0))
+    assert e.error_bits() & 8
+    e.close()

@@ -7,7 +7,8 @@ parameter files and structures (fixtures).  The reference's seeded outputs
 (tests/remctest_{CPU,GPU}.tgz) give the file layout, which must match exactly, and one
 sample each of the acceptance and exchange statistics, which must fall within the
 spread of independent runs here (the random streams differ: GSL MT19937 there,
-Philox here).
+Philox here): final acceptance ratios, exchange ratio, fraction bound, and the mean
+potential of the samples at each temperature (boundconformations).
 """
 import ctypes
 import os
@@ -48,6 +49,18 @@ def workdir(tmp_path_factory, refdata):
     return d
 
 
+def sampled_energy_by_temperature(path):
+    """Mean sampled replica potential per temperature label of a boundconformations file
+    (lines "step; E_nc (E); T" followed by the sample's PDB name)."""
+    per_t = {}
+    for ln in open(path).read().splitlines()[2:]:
+        if ";" not in ln:
+            continue
+        f = ln.split(";")
+        per_t.setdefault(f[2].strip(), []).append(float(f[1].split("(")[1].split(")")[0]))
+    return {t: (float(np.mean(v)), len(v)) for t, v in per_t.items()}
+
+
 def config(refdata, prefix, seed):
     text = refdata["remctestfile"].replace("prefix remctest", "prefix %s\nseed %d" % (prefix, seed))
     return text
@@ -66,7 +79,16 @@ def test_output_files_match_reference_layout(workdir, refdata):
     ex = open(out / "exchange_freq").read().splitlines()
     assert ex[0] == "# Iteration continous_ratio, inst_ratio" and len(ex) - 1 == gold["exchange_rows"]
     assert open(out / "fileindex").read().splitlines() == gold["fileindex"]
-    assert open(out / "boundconformations").read().splitlines()[:2] == gold["boundconformations_header"]
+    bc = open(out / "boundconformations").read().splitlines()
+    assert bc[:2] == gold["boundconformations_header"]
+    # one sample per replica and block (sampling every 10 steps, 10-step blocks): the
+    # reference's line pairs "step; E_nc (E); T" + PDB name, steps 0, 10, ..., 990
+    assert len(bc) - 2 == 2 * 5 * 100
+    steps = sorted({int(ln.split(";")[0]) for ln in bc[2::2]})
+    assert steps == list(range(0, 1000, 10))
+    assert all(ln.startswith("output/remctest_0/pdb/sample_") for ln in bc[3::2])
+    counts = {t: n for t, (_, n) in sampled_energy_by_temperature(out / "boundconformations").items()}
+    assert counts == gold["sampled_energy_count_by_temperature"]
     # row labels: MC step counts of the blocks, then the closing row
     labels = [int(ln.split(":")[0]) for ln in acc_lines[2:] if ":" in ln]
     assert labels == list(range(10, 1001, 10))
@@ -74,7 +96,7 @@ def test_output_files_match_reference_layout(workdir, refdata):
 
 
 def test_statistics_within_spread_of_reference(workdir, refdata):
-    finals, exch, fbound = [], [], []
+    finals, exch, fbound, energies = [], [], [], []
     for seed in range(1, 33):
         prefix = "stat%d" % seed
         (workdir / prefix).write_text(config(refdata, prefix, seed))
@@ -85,6 +107,7 @@ def test_statistics_within_spread_of_reference(workdir, refdata):
         _, fb = parse_rows(out / "fractionBound")
         fbound.append(fb[-1][1::2])
         exch.append(float(open(out / "exchange_freq").read().splitlines()[-1].split()[1]))
+        energies.append(sampled_energy_by_temperature(out / "boundconformations"))
     finals = np.array(finals)
     mean, sd = finals.mean(0), finals.std(0, ddof=1)
     em, es = np.mean(exch), np.std(exch, ddof=1)
@@ -96,3 +119,9 @@ def test_statistics_within_spread_of_reference(workdir, refdata):
         assert abs(g["exchange_final_cumulative"] - em) / max(es, 0.01) < 4.5, (arch, g["exchange_final_cumulative"],
                                                                                   em, es)
         assert np.allclose(np.array(g["fraction_final_cumulative"]), np.mean(fbound, 0), atol=0.05)
+        # per-temperature mean energy of the reference's samples against the spread of
+        # the 32 runs' means at the same temperature
+        for t, e_ref in g["sampled_energy_mean_by_temperature"].items():
+            ours = np.array([run[t][0] for run in energies])
+            z = abs(e_ref - ours.mean()) / max(ours.std(ddof=1), 0.05)
+            assert z < 4.5, (arch, t, e_ref, ours.mean(), ours.std(ddof=1))
