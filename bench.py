@@ -354,19 +354,30 @@ def dropin_leg(args, torch, flush, wl, peak_tflops):
     stream = torch.cuda.Stream()
     args_async = (ctypes.c_void_p(dp.data_ptr()), ctypes.c_void_p(dm.data_ptr()), None, None, None, None,
                   ctypes.c_void_p(out.data_ptr()), rs, 32, P, 0, ctypes.c_void_p(stream.cuda_stream))
-    reps = 20
+    reps, burst = 20, 20
     with torch.cuda.stream(stream):
         for _ in range(3):
             L.CUDA_EonDevice_async(*args_async)
-        times = []
+        times, singles = [], []
         for _ in range(reps):
+            # a burst of calls enqueued back to back (as replicas issue them on a stream):
+            # the host's launch work overlaps the previous call's kernel, so the events
+            # time the kernels; the packed arrays (113 KB) stay in L2 as they do for a caller
             flush.fill_(1.0)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(burst):
+                L.CUDA_EonDevice_async(*args_async)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / burst)
+            # one call alone between the events (launch latency included)
+            flush.fill_(1.0)
             e0.record(stream)
             L.CUDA_EonDevice_async(*args_async)
             e1.record(stream)
             e1.synchronize()
-            times.append(e0.elapsed_time(e1))
+            singles.append(e0.elapsed_time(e1))
     cgppd_gb300.check("dropin leg")
     k_ms = float(np.median(times))
     res = ctypes.c_double(0.0)
@@ -381,7 +392,9 @@ def dropin_leg(args, torch, flush, wl, peak_tflops):
     L.cgppd_aminoacids_destroy(a)
     tflops = pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
     return {"entry": "CUDA_EonDevice(_async)", "kernel": "k_tile_energy", "workload": wl.name + ", replica 0",
-            "residues": N, "padded": P, "pairs_per_call": pairs, "kernel_ms": k_ms, "sync_call_ms": sync_ms,
+            "residues": N, "padded": P, "pairs_per_call": pairs, "kernel_ms": k_ms,
+            "kernel_ms_note": "median over 20 bursts of 20 back-to-back async calls on one stream, per call",
+            "single_call_ms": float(np.median(singles)), "sync_call_ms": sync_ms,
             "pair_evals_per_s": pairs / (k_ms / 1000.0), "achieved_tflops": tflops, "frac": tflops / peak_tflops,
             "energy_kcal": res.value}
 

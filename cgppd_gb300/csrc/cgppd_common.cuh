@@ -51,6 +51,27 @@ __device__ __forceinline__ void ff_add(FF &a, float b)
 
 __device__ __forceinline__ double ff_value(const FF &a) { return (double)a.hi + (double)a.lo; }
 
+// a += b for two float-float values (TwoSum of the high parts, the low parts added).
+__device__ __forceinline__ void ff_add_ff(FF &a, FF b)
+{
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float err = (a.hi - (s - bb)) + (b.hi - bb);
+    a.hi = s;
+    a.lo += err + b.lo;
+}
+
+// Sum over the warp (butterfly: every lane ends with the same value, in a fixed order).
+__device__ __forceinline__ FF ff_warp_sum(FF v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        FF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        ff_add_ff(v, w);
+    }
+    return v;
+}
+
 // ------------------------------------------------------------------ geometry
 __device__ __forceinline__ float min_image(float d, float L, float invL)
 {

@@ -213,25 +213,6 @@ __device__ __forceinline__ Lists global_lists(const EngineArgs &a)
 
 // ------------------------------------------------------------------ helpers
 
-__device__ __forceinline__ void ff_add_ff(FF &a, FF b)
-{
-    float s = a.hi + b.hi;
-    float bb = s - a.hi;
-    float err = (a.hi - (s - bb)) + (b.hi - bb);
-    a.hi = s;
-    a.lo += err + b.lo;
-}
-
-__device__ __forceinline__ FF ff_warp_sum(FF v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        FF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-        ff_add_ff(v, w);
-    }
-    return v;
-}
-
 __device__ __forceinline__ double warp_sum_d(double v)
 {
 #pragma unroll

@@ -11,7 +11,9 @@ and delayed-acceptance screening inside the engine.
 * the error threshold trips the fallback to the plain test, and a wildly wrong network
   leaves the running totals exact;
 * training lowers the held-out error, and the trained network's first stage saves exact
-  pair work relative to the plain engine.
+  pair work relative to the plain engine;
+* screening with a trained network, and with that network's output negated, samples the
+  plain engine's distribution (per-temperature mean energy over 16 simulations).
 """
 import numpy as np
 import pytest
@@ -236,3 +238,78 @@ def test_trained_surrogate_skips_exact_work():
     plain.close()
     da.close()
     s.close()
+
+
+def two_copy_workload(n_sims):
+    """`n_sims` independent copies of one small system: two copies of the c4 protein 30 A
+    apart in a 60 A box, 8 temperatures 288-450 K (contacts form and break within a few
+    thousand steps, so both arms below reach the same stationary state quickly)."""
+    wl4 = workloads.make("c4")
+    base = wl4.sims[0].molecules[0]
+    m2 = workloads.Molecule(base.xyz + np.float32([30.0, 0.0, 0.0]), base.types, base.charges, base.radii)
+    sims = [workloads.Simulation([base, m2], 60.0, workloads.ladder(288.0, 450.0, 8),
+                                 workloads.ladder(0.5, 2.0, 8), workloads.ladder(0.2, 0.2, 8))
+            for _ in range(n_sims)]
+    return workloads.Workload("two copies", sims, wl4.lj_raw, seed=wl4.seed)
+
+
+def mean_energy_by_temperature(e, n_sims, blocks, steps):
+    """Per simulation and temperature index: the mean potential at the ends of `blocks`
+    exchange blocks."""
+    acc = np.zeros((n_sims, 8))
+    for _ in range(blocks):
+        e.run(1, steps, exchange_after_last=True)
+        for s in range(n_sims):
+            rep = e.replicas(s)
+            acc[s, rep["tindex"]] += rep["potential"]
+    return acc / blocks
+
+
+def test_screening_samples_the_plain_distribution():
+    # Delayed acceptance changes which proposals are evaluated exactly, not the sampled
+    # distribution: from the same equilibrated states, the plain engine, the engine
+    # screened by a trained network and the engine screened by the same network with its
+    # output negated (a first stage that prefers uphill moves) give the same mean energy at
+    # every temperature within the spread of 16 independent simulations each.
+    S, steps = 16, 500
+    wl = two_copy_workload(S)
+    burn = eng.from_workload(wl, cluster=4, threads=256)
+    burn.run(40, steps, exchange_after_last=True)
+    s, hist = sg.train_on_engine(burn, 0, n_samples=262144, blocks=4, steps_per_block=steps, epochs=4, batch=8192)
+    snap = []
+    for k in range(S):
+        rep = burn.replicas(k)
+        snap.append([(int(rep["tindex"][r]), burn.state(k, r)) for r in range(8)])
+    flipped = sg.Surrogate(batch=8192, seed=3)
+    p = s.params.copy()
+    for name in ("w5", "b5"):  # (offset, length) of the output layer's weights and bias
+        off, n = mlp.OFF[name]
+        p[off:off + n] *= -1.0
+    flipped.params = p
+
+    def arm(net):
+        e = eng.from_workload(wl, cluster=4, threads=256)
+        for k in range(S):
+            for t, (xyz, rel, cen) in snap[k]:
+                e.set_state(k, t, xyz, rel, cen)  # slot t holds temperature index t
+        e.recompute(write_state=True)
+        if net is not None:
+            assert sg.attach(e, net, rmse_threshold=1e30) == S
+        e.run(10, steps, exchange_after_last=True)
+        m = mean_energy_by_temperature(e, S, 60, steps)
+        st = sg.stats(e, 0) if net is not None else None
+        assert np.allclose(e.recompute(False), np.concatenate([e.replicas(k)["potential"] for k in range(S)]),
+                           rtol=1e-6, atol=1e-6)
+        e.close()
+        return m, st
+
+    plain, _ = arm(None)
+    for net in (s, flipped):
+        m, st = arm(net)
+        assert st["screening"] == 1 and st["stage1_reject"] > 0
+        se = np.sqrt(plain.var(0, ddof=1) / S + m.var(0, ddof=1) / S)
+        z = np.abs(plain.mean(0) - m.mean(0)) / np.maximum(se, 1e-3)
+        assert np.all(z < 4.5), (plain.mean(0), m.mean(0), se)
+    burn.close()
+    s.close()
+    flipped.close()
