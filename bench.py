@@ -307,7 +307,37 @@ def surrogate_leg(args, torch, flush):
                            "online_rmse_kcal": a1["rmse"]}}
     always.close()
     s.close()
+    out["crowded_bound"] = crowded_screen_bound(args, torch, flush)
     return out
+
+
+def crowded_screen_bound(args, torch, flush):
+    """What any delayed-acceptance screen can gain on the crowded configuration: its first
+    stage saves only the exact evaluations of proposals it rejects, and a correct first
+    stage rejects at most what the exact test rejects, so the effective speed-up of a
+    free, perfect screen is 1 / acceptance.  Measured on the plain engine (acceptance per
+    temperature over 10 exchange blocks after 5 blocks of equilibration)."""
+    from cgppd_gb300 import engine as eng
+    from cgppd_gb300 import workloads
+    wl = workloads.make("c2")
+    e = eng.from_workload(wl)
+    e.run(5, args.block, True)
+    r0 = e.replicas(0)
+    e.run(10, args.block, True)
+    e.synchronize()
+    r1 = e.replicas(0)
+    # the counters travel with the temperature on exchange: totals per ladder index
+    before = {int(t): (a, n) for t, a, n in zip(r0["tindex"], r0["totalAccept"], r0["totalAcceptReject"])}
+    acc = [0.0] * len(r1["tindex"])
+    for t, a, n in zip(r1["tindex"], r1["totalAccept"], r1["totalAcceptReject"]):
+        a0, n0 = before[int(t)]
+        acc[int(t)] = float(a - a0) / max(1, int(n - n0))
+    e.close()
+    return {"workload": wl.name, "acceptance_by_temperature": acc, "acceptance_mean": float(np.mean(acc)),
+            "max_speedup_of_any_screen": 1.0 / float(np.mean(acc)),
+            "note": "a first stage can skip only the exact evaluations of proposals it rejects; a correct one "
+                    "rejects at most the ones the exact test rejects, so even a free, perfect screen gains at "
+                    "most 1 / acceptance"}
 
 
 # ------------------------------------------------------------------ drop-in energy module
