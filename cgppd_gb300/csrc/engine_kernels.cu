@@ -357,16 +357,16 @@ __device__ __forceinline__ void load_table(float *s_table, const float *table, i
 // `col` the table column of b's type (col[type_a * kTableStride]).  The LJ term is
 // u = (-4 Eij) s6 (s6 - 1), and 2 Eij - u on the repulsive branch (Eij > 0, s6 > 1/2),
 // the same values as lj_term with one multiplication less (power-of-two scaling).
-// MI = false skips the minimum image: the caller has already moved b to the periodic
-// image that every pair of the two molecules takes (see the per-step molecule shifts in
-// k_mc), so a - b is the minimum-image difference itself.
-template <bool DH, bool MI>
+// MI: the axes (bit 0 x, 1 y, 2 z) that take the minimum image; on the others the caller
+// has already moved b to the periodic image that every pair takes (see the inter-pair
+// loop of k_mc), so a - b is the minimum-image difference itself.
+template <bool DH, int MI>
 __device__ __forceinline__ float pair_term(float4 a, float2 qa, float4 b, float qb, const float *col, float L,
                                            float invL)
 {
-    const float dx = MI ? min_image(a.x - b.x, L, invL) : a.x - b.x;
-    const float dy = MI ? min_image(a.y - b.y, L, invL) : a.y - b.y;
-    const float dz = MI ? min_image(a.z - b.z, L, invL) : a.z - b.z;
+    const float dx = (MI & 1) ? min_image(a.x - b.x, L, invL) : a.x - b.x;
+    const float dy = (MI & 2) ? min_image(a.y - b.y, L, invL) : a.y - b.y;
+    const float dz = (MI & 4) ? min_image(a.z - b.z, L, invL) : a.z - b.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float inv_r = rsqrt_sfu(r2);
     const float m4e = col[__float_as_int(qa.y) * kTableStride];
@@ -385,14 +385,14 @@ template <bool DH = true>
 __device__ __forceinline__ float pair_kcal(float4 a, float2 qa, float4 b, float2 qb, const float *table, float L,
                                            float invL)
 {
-    return pair_term<DH, true>(a, qa, b, qb.x, table + __float_as_int(qb.y), L, invL);
+    return pair_term<DH, 7>(a, qa, b, qb.x, table + __float_as_int(qb.y), L, invL);
 }
 
 // Pair terms of residues i = i0, i0 + g, ... < i1 of the mover (records ipv / iqv) with
 // one residue b of another molecule: four independent partial sums, folded into the
 // float-float accumulator every 32 terms.  Returns the first index of the sequence at or
 // past i1 (where the next span of the same sequence starts).
-template <bool DH, bool MI>
+template <bool DH, int MI>
 __device__ __forceinline__ int pair_span(const float4 *ipv, const float2 *iqv, int i0, int i1, int g, float4 b,
                                           float qb, const float *col, float L, float invL, FF &acc, float &p0,
                                           float &p1, float &p2, float &p3)
@@ -412,6 +412,21 @@ __device__ __forceinline__ int pair_span(const float4 *ipv, const float2 *iqv, i
     for (; i < i1; i += g)
         p0 += pair_term<DH, MI>(ipv[i], iqv[i], b, qb, col, L, invL);
     return i;
+}
+
+// Every pair of the mover (its charged residues first: the full term, then the
+// Lennard-Jones part alone) with the residue b, residues i = sub, sub + g, ... of the
+// mover, into acc.
+template <int MI>
+__device__ __forceinline__ void mover_spans(const float4 *ipv, const float2 *iqv, int sub, int nqm, int n, int g,
+                                            float4 b, float qb, const float *col, float L, float invL, FF &acc)
+{
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+    const int i2 = pair_span<true, MI>(ipv, iqv, sub, nqm, g, b, qb, col, L, invL, acc, p0, p1, p2, p3);
+    ff_add(acc, (p0 + p1) + (p2 + p3));
+    p0 = p1 = p2 = p3 = 0.f;
+    pair_span<false, MI>(ipv, iqv, i2, n, g, b, qb, col, L, invL, acc, p0, p1, p2, p3);
+    ff_add(acc, (p0 + p1) + (p2 + p3));
 }
 
 // Repulsive crowder pair in kcal/mol, the reference's REPULSIVE_CROWDING build
@@ -1450,9 +1465,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         // the mover's bounding radius inside the half box around the centre on every
         // axis, no mover residue is more than half a box from it, so the per-pair rule
         // (src/CudaFunctions.cu:321-333) takes exactly that image for every pair and the
-        // loop takes the plain differences; warps with a j in the outer shell keep the
-        // per-pair minimum image.  (Flexible movers have no fixed radius: always the
-        // per-pair rule.)
+        // loop takes the plain differences; on an axis where some j of the warp lies in the
+        // outer shell the warp keeps the per-pair minimum image for that axis.  (Flexible
+        // movers have no fixed radius: always the per-pair rule.)
         const float hlim = (L != 0.0f && !flexmol) ? 0.5f * L - (s_rad[m] + kImageMargin) : -1.0f;
         auto stat_of = [&](int j) -> float4 {
             return RES ? make_float4(0.f, Q[j].w, __int_as_float((int)TY[j]), 0.f) : ST[j];
@@ -1475,15 +1490,16 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 nsj = stat_of(jn);
             }
             // j's image nearest the mover's centre (the minimum-image rule applied once;
-            // exactly pj where that image is pj itself); the warp takes the loop without a
-            // per-pair minimum image when that image is inner for all of its j
+            // exactly pj where that image is pj itself)
             const float kx = __fadd_rn(__fmaf_rn(pj.x - mv.wcx, invL, 12582912.0f), -12582912.0f);
             const float ky = __fadd_rn(__fmaf_rn(pj.y - mv.wcy, invL, 12582912.0f), -12582912.0f);
             const float kz = __fadd_rn(__fmaf_rn(pj.z - mv.wcz, invL, 12582912.0f), -12582912.0f);
             const float bx = fmaf(-L, kx, pj.x), by = fmaf(-L, ky, pj.y), bz = fmaf(-L, kz, pj.z);
-            const bool inner = L == 0.0f || (fabsf(bx - mv.wcx) < hlim && fabsf(by - mv.wcy) < hlim &&
-                                             fabsf(bz - mv.wcz) < hlim);
-            const bool fast = __all_sync(0xffffffffu, inner || !valid || crowd);
+            // the axes on which some j of the warp lies outside the inner region
+            const bool use = valid && !crowd && L != 0.0f;
+            const int outer = (__any_sync(0xffffffffu, use && !(fabsf(bx - mv.wcx) < hlim)) ? 1 : 0) |
+                              (__any_sync(0xffffffffu, use && !(fabsf(by - mv.wcy) < hlim)) ? 2 : 0) |
+                              (__any_sync(0xffffffffu, use && !(fabsf(bz - mv.wcz) < hlim)) ? 4 : 0);
             FF acc{0.f, 0.f};
             if (valid && crowd) {
                 float p0 = 0.f;
@@ -1501,25 +1517,20 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 const float qj = sj.y;
                 const float *col = s_table + __float_as_int(sj.z);
                 const float sw = RES ? pj.w : sj.x;
-                // four independent partial sums (instruction-level parallelism), folded
-                // into the float-float accumulator every 32 terms
-                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-                if (fast) {
-                    const float4 rj = make_float4(bx, by, bz, sw);
-                    const int i2 = pair_span<true, false>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1,
-                                                          p2, p3);
-                    ff_add(acc, (p0 + p1) + (p2 + p3));
-                    p0 = p1 = p2 = p3 = 0.f;
-                    pair_span<false, false>(ipv, iqv, i2, n, g, rj, qj, col, L, invL, acc, p0, p1, p2, p3);
-                } else {
-                    const float4 rj = make_float4(pj.x, pj.y, pj.z, sw);
-                    const int i2 = pair_span<true, true>(ipv, iqv, sub, nqm, g, rj, qj, col, L, invL, acc, p0, p1,
-                                                         p2, p3);
-                    ff_add(acc, (p0 + p1) + (p2 + p3));
-                    p0 = p1 = p2 = p3 = 0.f;
-                    pair_span<false, true>(ipv, iqv, i2, n, g, rj, qj, col, L, invL, acc, p0, p1, p2, p3);
-                }
-                ff_add(acc, (p0 + p1) + (p2 + p3));
+                // j's image nearest the mover's centre; the minimum image per pair only on
+                // the axes where the warp needs it (most outer warps are outer on one axis)
+                const float4 rj = make_float4(bx, by, bz, sw);
+                if (outer == 0)
+                    mover_spans<0>(ipv, iqv, sub, nqm, n, g, rj, qj, col, L, invL, acc);
+                else if (outer == 1)
+                    mover_spans<1>(ipv, iqv, sub, nqm, n, g, rj, qj, col, L, invL, acc);
+                else if (outer == 2)
+                    mover_spans<2>(ipv, iqv, sub, nqm, n, g, rj, qj, col, L, invL, acc);
+                else if (outer == 4)
+                    mover_spans<4>(ipv, iqv, sub, nqm, n, g, rj, qj, col, L, invL, acc);
+                else
+                    mover_spans<7>(ipv, iqv, sub, nqm, n, g, make_float4(pj.x, pj.y, pj.z, sw), qj, col, L, invL,
+                                   acc);
             }
             // segmented tree sum towards the group's first lane: after the step with offset
             // d, lane sub holds the lanes [sub, min(sub + 2d, g)) of its group
