@@ -62,6 +62,27 @@ __device__ __forceinline__ float frac_int(float w, float &ip)
     return w - ip;
 }
 
+// 1/x on the SFU (PTX rcp.approx.ftz.f32, max relative error about 2^-23).
+__device__ __forceinline__ float rcp_sfu(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// The Lennard-Jones part of lj_term with the table value m4e = -4 Eij (RT units) and the
+// mixed radius sigma_ij: u = m4e s6 (s6 - 1), and 2 Eij - u on the repulsive branch
+// (Eij > 0, s6 > 1/2); one multiplication less than lj_term.
+__device__ __forceinline__ float lj_m4(float m4e, float sigma_ij, float inv_r2)
+{
+    const float s2 = sigma_ij * sigma_ij * inv_r2;
+    const float s6 = s2 * s2 * s2;
+    float u = m4e * fmaf(s6, s6, -s6);
+    if (m4e < 0.0f && s6 > 0.5f)
+        u = fmaf(-0.5f, m4e, -u);
+    return u;
+}
+
 // Folds one residue's exclusion keys into its tile's ranges (warp reductions, then one
 // shared atomic per warp and key) and flags.  Ranges are of the keys' bit patterns:
 // two sets of floats whose bit-pattern ranges are disjoint share no value.
@@ -112,6 +133,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     __shared__ float4 s_xk[kTile];
     __shared__ float4 s_xm[kTile];
     __shared__ float s_eij[400];
+    __shared__ float s_m4[400];   // -4 Eij in RT units (the clean-tile loop's form)
     __shared__ FF s_red[2][kWarps];
     __shared__ bool s_last;
     // the x tile again in charged-first order (position + radius, charge + type) for
@@ -136,7 +158,11 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     const int yl = t & (kTile - 1), half = t / kTile;  // y residue, half of the x tile
 
     for (int k = t; k < 400; k += kThreads)
-        s_eij[k] = kLambda * (lj_raw[k] - kE0);  // Eij in RT units, as the kernel forms it
+    {
+        const float e = kLambda * (lj_raw[k] - kE0);  // Eij in RT units, as the kernel forms it
+        s_eij[k] = e;
+        s_m4[k] = -4.0f * e;
+    }
     if (t < 16)
         s_keys[t >> 3][t & 7] = (t & 1) ? -1 : 0x7fffffff;  // empty ranges: min > max
     if (t < 2)
@@ -208,7 +234,9 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
             const bool q = (qb >> (t & 31)) & 1u;
             const int k = q ? before + __popc(below) : nqx + (t - before - __popc(below));
             const float4 xm = s_xm[t];
-            s_pq[k] = s_px[t];
+            float4 pw = s_px[t];
+            pw.w *= 0.5f;  // half the radius: sigma_ij = half_y + half_x
+            s_pq[k] = pw;
             s_qt[k] = make_float2(xm.x, xm.y);
         }
         __syncthreads();
@@ -236,7 +264,10 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         const float yq = my.y, ys = my.z;
         if (clean) {
             // the two threads of a y residue take alternate x residues: charged ones with
-            // the full term, then the rest with the Lennard-Jones part alone
+            // the full term, then the rest with the Lennard-Jones part alone (1/r^2 from
+            // the SFU reciprocal: no 1/r needed there)
+            const float *m4row = s_m4 + 20 * yt;
+            const float yh = 0.5f * ys;
             float l0 = 0.f, l1 = 0.f, d0 = 0.f;
             int j = half, cnt = 0;
             for (; j < nqx; j += 2) {
@@ -247,7 +278,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
                 const float dz = min_image(py.z - px.z, L, invL);
                 const float r2 = fmaf(dx, dx, fmaf(dyy, dyy, dz * dz));
                 const float inv_r = rsqrt_sfu(r2);
-                l0 += lj_term(erow[__float_as_int(qt.y)], (ys + px.w) * 0.5f, inv_r * inv_r);
+                l0 += lj_m4(m4row[__float_as_int(qt.y)], yh + px.w, inv_r * inv_r);
                 d0 += dh_term(yq * qt.x, r2 * inv_r, inv_r);
                 if (++cnt == 32) {
                     ff_add(lj, l0);
@@ -267,9 +298,8 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
                 const float ay = min_image(py.y - pa.y, L, invL), by = min_image(py.y - pb.y, L, invL);
                 const float az = min_image(py.z - pa.z, L, invL), bz = min_image(py.z - pb.z, L, invL);
                 const float ra = fmaf(ax, ax, fmaf(ay, ay, az * az)), rb = fmaf(bx, bx, fmaf(by, by, bz * bz));
-                const float ia = rsqrt_sfu(ra), ib = rsqrt_sfu(rb);
-                l0 += lj_term(erow[ta], (ys + pa.w) * 0.5f, ia * ia);
-                l1 += lj_term(erow[tb], (ys + pb.w) * 0.5f, ib * ib);
+                l0 += lj_m4(m4row[ta], yh + pa.w, rcp_sfu(ra));
+                l1 += lj_m4(m4row[tb], yh + pb.w, rcp_sfu(rb));
                 if (++cnt == 16) {
                     ff_add(lj, l0 + l1);
                     l0 = l1 = 0.f;
@@ -281,8 +311,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
                 const float ax = min_image(py.x - pa.x, L, invL);
                 const float ay = min_image(py.y - pa.y, L, invL);
                 const float az = min_image(py.z - pa.z, L, invL);
-                const float ia = rsqrt_sfu(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-                l0 += lj_term(erow[__float_as_int(s_qt[j].y)], (ys + pa.w) * 0.5f, ia * ia);
+                l0 += lj_m4(m4row[__float_as_int(s_qt[j].y)], yh + pa.w, rcp_sfu(fmaf(ax, ax, fmaf(ay, ay, az * az))));
             }
             ff_add(lj, l0 + l1);
         }
