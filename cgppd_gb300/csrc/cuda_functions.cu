@@ -7,9 +7,10 @@
 // crowder).  The pair rules are those of the reference's flexible-linker build.
 //
 // Kernel: one CTA per (y-tile, x-tile) pair of 128-residue tiles on or above the
-// diagonal.  Tile pairs that cannot hold an excluded pair (checked per CTA from the key
-// ranges of the two tiles) take a loop without exclusion tests over the x tile in
-// charged-first order, with the Debye-Hueckel term for charged x residues only.  The x tile is decoded once into shared memory (position and radius; the
+// diagonal.  The x tile is copied in charged-first order, so the Debye-Hueckel term is
+// taken for charged x residues only; tile pairs that cannot hold an excluded pair
+// (checked per CTA from the key ranges of the two tiles) run that loop without exclusion
+// tests, the others with the tests per pair (the crowder forms keep a general loop).  The x tile is decoded once into shared memory (position and radius; the
 // exclusion keys of its w fields; charge, type and flags) next to the 20x20 table; two
 // threads own each y residue and sweep one half of the x tile each.  Pair terms are
 // FP32, summed per 32 pairs in two alternating partial sums and folded into
@@ -83,6 +84,93 @@ __device__ __forceinline__ float lj_m4(float m4e, float sigma_ij, float inv_r2)
     return u;
 }
 
+// What the charged-first loop needs of its y residue.
+struct PairCtx {
+    float4 py;
+    float yh, yq;             // half radius, charge
+    const float *m4row;       // -4 Eij (RT units) row of the y type
+    float L, invL;
+    int yl, x0, y;            // y's place in its tile, the x tile's first index, y's index
+    bool diag, near;
+    float ydom, ybond, ychain;
+    bool ydom_nz, ybond_nz;
+};
+
+// The y residue against the x tile in charged-first order, the two threads of a y
+// residue taking alternate x residues: charged ones with the full term, then the rest
+// with the Lennard-Jones part alone (1/r^2 from the SFU reciprocal: no 1/r needed
+// there).  TESTED: the pairs the reference excludes (same rigid domain, same bond,
+// chain neighbours |x - y| < 4, padding, the diagonal tile's lower half) are evaluated
+// and selected away, with the rules of the general loop.
+template <bool TESTED>
+__device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const float4 *s_pq, const float2 *s_qt,
+                                                    const float4 *s_qk, int nqx, int half, FF &lj, FF &dh)
+{
+    auto excluded = [&](int j) -> bool {
+        if (!TESTED)
+            return false;
+        const float4 k = s_qk[j];
+        const int oi = __float_as_int(k.w), xi = oi & 0xffff;
+        return (oi >> 16) != 0 || (c.diag && xi <= c.yl) || (c.ydom_nz && k.x == c.ydom) ||
+               (c.ybond_nz && k.y == c.ybond) || (c.near && k.z == c.ychain && abs(c.x0 + xi - c.y) < 4);
+    };
+    const float4 py = c.py;
+    const float L = c.L, invL = c.invL;
+    float l0 = 0.f, l1 = 0.f, d0 = 0.f;
+    int j = half, cnt = 0;
+    for (; j < nqx; j += 2) {
+        const float4 px = s_pq[j];
+        const float2 qt = s_qt[j];
+        const float dx = min_image(py.x - px.x, L, invL);
+        const float dyy = min_image(py.y - px.y, L, invL);
+        const float dz = min_image(py.z - px.z, L, invL);
+        const float r2 = fmaf(dx, dx, fmaf(dyy, dyy, dz * dz));
+        const float inv_r = rsqrt_sfu(r2);
+        const float u = lj_m4(c.m4row[__float_as_int(qt.y)], c.yh + px.w, inv_r * inv_r);
+        const float d = dh_term(c.yq * qt.x, r2 * inv_r, inv_r);
+        const bool ex = excluded(j);
+        l0 += ex ? 0.f : u;
+        d0 += ex ? 0.f : d;
+        if (++cnt == 32) {
+            ff_add(lj, l0);
+            ff_add(dh, d0);
+            l0 = d0 = 0.f;
+            cnt = 0;
+        }
+    }
+    ff_add(lj, l0);
+    ff_add(dh, d0);
+    l0 = 0.f;
+    cnt = 0;
+    for (; j + 2 < kTile; j += 4) {
+        const float4 pa = s_pq[j], pb = s_pq[j + 2];
+        const int ta = __float_as_int(s_qt[j].y), tb = __float_as_int(s_qt[j + 2].y);
+        const float ax = min_image(py.x - pa.x, L, invL), bx = min_image(py.x - pb.x, L, invL);
+        const float ay = min_image(py.y - pa.y, L, invL), by = min_image(py.y - pb.y, L, invL);
+        const float az = min_image(py.z - pa.z, L, invL), bz = min_image(py.z - pb.z, L, invL);
+        const float ra = fmaf(ax, ax, fmaf(ay, ay, az * az)), rb = fmaf(bx, bx, fmaf(by, by, bz * bz));
+        const float ua = lj_m4(c.m4row[ta], c.yh + pa.w, rcp_sfu(ra));
+        const float ub = lj_m4(c.m4row[tb], c.yh + pb.w, rcp_sfu(rb));
+        l0 += excluded(j) ? 0.f : ua;
+        l1 += excluded(j + 2) ? 0.f : ub;
+        if (++cnt == 16) {
+            ff_add(lj, l0 + l1);
+            l0 = l1 = 0.f;
+            cnt = 0;
+        }
+    }
+    for (; j < kTile; j += 2) {
+        const float4 pa = s_pq[j];
+        const float ax = min_image(py.x - pa.x, L, invL);
+        const float ay = min_image(py.y - pa.y, L, invL);
+        const float az = min_image(py.z - pa.z, L, invL);
+        const float ra = fmaf(ax, ax, fmaf(ay, ay, az * az));
+        const float ua = lj_m4(c.m4row[__float_as_int(s_qt[j].y)], c.yh + pa.w, rcp_sfu(ra));
+        l0 += excluded(j) ? 0.f : ua;
+    }
+    ff_add(lj, l0 + l1);
+}
+
 // Folds one residue's exclusion keys into its tile's ranges (warp reductions, then one
 // shared atomic per warp and key) and flags.  Ranges are of the keys' bit patterns:
 // two sets of floats whose bit-pattern ranges are disjoint share no value.
@@ -140,6 +228,9 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     // tile pairs without any excluded pair
     __shared__ float4 s_pq[kTile];
     __shared__ float2 s_qt[kTile];
+    // ... and its exclusion keys (domain, bond, chain, original index | padding << 16) for
+    // tile pairs that may hold excluded pairs (default potential)
+    __shared__ float4 s_qk[kTile];
     __shared__ unsigned s_qballot[kTile / 32];
     // key ranges of the two tiles, [x, y][nonzero domain min/max, nonzero bond min/max,
     // chain min/max, molecule min/max] as float bits, and [x, y] flags: bit 0 padding,
@@ -219,8 +310,11 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         clean = clean && ranges_disjoint(s_keys[0][0], s_keys[0][1], s_keys[1][0], s_keys[1][1]) &&
                 ranges_disjoint(s_keys[0][2], s_keys[0][3], s_keys[1][2], s_keys[1][3]) &&
                 (tx - ty >= 2 || ranges_disjoint(s_keys[0][4], s_keys[0][5], s_keys[1][4], s_keys[1][5]));
+    // Other tile pairs of the default potential take the same charged-first loop with the
+    // exclusion tests per pair; the crowder forms keep the general loop.
+    const bool tested = !clean && !kNC && !kRC;
     int nqx = 0;
-    if (clean) {
+    if (clean || tested) {
         // the x tile in charged-first order (stable): the Debye-Hueckel term is then taken
         // for the charged x residues only
         int before = 0;
@@ -238,6 +332,8 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
             pw.w *= 0.5f;  // half the radius: sigma_ij = half_y + half_x
             s_pq[k] = pw;
             s_qt[k] = make_float2(xm.x, xm.y);
+            const float4 xk = s_xk[t];
+            s_qk[k] = make_float4(xk.x, xk.y, xk.z, __int_as_float(t | ((__float_as_int(xm.z) & 1) << 16)));
         }
         __syncthreads();
     }
@@ -262,61 +358,16 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         }
         const float *erow = s_eij + 20 * yt;
         const float yq = my.y, ys = my.z;
-        if (clean) {
-            // the two threads of a y residue take alternate x residues: charged ones with
-            // the full term, then the rest with the Lennard-Jones part alone (1/r^2 from
-            // the SFU reciprocal: no 1/r needed there)
-            const float *m4row = s_m4 + 20 * yt;
-            const float yh = 0.5f * ys;
-            float l0 = 0.f, l1 = 0.f, d0 = 0.f;
-            int j = half, cnt = 0;
-            for (; j < nqx; j += 2) {
-                const float4 px = s_pq[j];
-                const float2 qt = s_qt[j];
-                const float dx = min_image(py.x - px.x, L, invL);
-                const float dyy = min_image(py.y - px.y, L, invL);
-                const float dz = min_image(py.z - px.z, L, invL);
-                const float r2 = fmaf(dx, dx, fmaf(dyy, dyy, dz * dz));
-                const float inv_r = rsqrt_sfu(r2);
-                l0 += lj_m4(m4row[__float_as_int(qt.y)], yh + px.w, inv_r * inv_r);
-                d0 += dh_term(yq * qt.x, r2 * inv_r, inv_r);
-                if (++cnt == 32) {
-                    ff_add(lj, l0);
-                    ff_add(dh, d0);
-                    l0 = d0 = 0.f;
-                    cnt = 0;
-                }
-            }
-            ff_add(lj, l0);
-            ff_add(dh, d0);
-            l0 = 0.f;
-            cnt = 0;
-            for (; j + 2 < kTile; j += 4) {
-                const float4 pa = s_pq[j], pb = s_pq[j + 2];
-                const int ta = __float_as_int(s_qt[j].y), tb = __float_as_int(s_qt[j + 2].y);
-                const float ax = min_image(py.x - pa.x, L, invL), bx = min_image(py.x - pb.x, L, invL);
-                const float ay = min_image(py.y - pa.y, L, invL), by = min_image(py.y - pb.y, L, invL);
-                const float az = min_image(py.z - pa.z, L, invL), bz = min_image(py.z - pb.z, L, invL);
-                const float ra = fmaf(ax, ax, fmaf(ay, ay, az * az)), rb = fmaf(bx, bx, fmaf(by, by, bz * bz));
-                l0 += lj_m4(m4row[ta], yh + pa.w, rcp_sfu(ra));
-                l1 += lj_m4(m4row[tb], yh + pb.w, rcp_sfu(rb));
-                if (++cnt == 16) {
-                    ff_add(lj, l0 + l1);
-                    l0 = l1 = 0.f;
-                    cnt = 0;
-                }
-            }
-            for (; j < kTile; j += 2) {
-                const float4 pa = s_pq[j];
-                const float ax = min_image(py.x - pa.x, L, invL);
-                const float ay = min_image(py.y - pa.y, L, invL);
-                const float az = min_image(py.z - pa.z, L, invL);
-                l0 += lj_m4(m4row[__float_as_int(s_qt[j].y)], yh + pa.w, rcp_sfu(fmaf(ax, ax, fmaf(ay, ay, az * az))));
-            }
-            ff_add(lj, l0 + l1);
+        if (clean || tested) {
+            const PairCtx c{py, 0.5f * ys, yq, s_m4 + 20 * yt, L, invL, yl, x0, y, diag, near, ydom, ybond, ychain,
+                            ydom_nz, ybond_nz};
+            if (clean)
+                charged_first_pairs<false>(c, s_pq, s_qt, s_qk, nqx, half, lj, dh);
+            else
+                charged_first_pairs<true>(c, s_pq, s_qt, s_qk, nqx, half, lj, dh);
         }
         const int jb0 = half * (kTile / 2);
-        for (int jb = jb0; !clean && jb < jb0 + kTile / 2; jb += 32) {
+        for (int jb = jb0; !clean && !tested && jb < jb0 + kTile / 2; jb += 32) {
             float l0 = 0.f, l1 = 0.f, d0 = 0.f, d1 = 0.f;
             // branch-free: every pair is evaluated and the excluded ones (padding, the
             // pair itself on the diagonal: possibly inf / NaN) are selected away
