@@ -8,6 +8,9 @@
    rounding of the acceptance probability -- the same decisions.  Positions are compared
    after whole blocks (tolerance 2e-3 A for the accumulated float rotations), potentials
    within 1e-5 relative, exchange decisions and counters exactly.
+3. Statistics: where float rotations part the trajectories from the reference loop's
+   double ones (C1), seeded runs of both sample the same per-temperature mean energies
+   and acceptance within statistical error.
 """
 import numpy as np
 import pytest
@@ -202,6 +205,55 @@ def test_flexible_and_rigid_clusters_match_oracle(config):
     e.run(2, 80)
     o.run(2, 80)
     compare_runs(e, o, traj_rel=REL if config != "c1" else 2e-4)
+
+
+def test_flexible_linker_statistics_match_oracle():
+    # C1's rigid and flex rotations run in float here and in double in the reference loop
+    # (src/Quaternion.cpp:95-112), so trajectories part after a few hundred steps.  What
+    # must not change is what they sample: per-temperature mean energies of independent
+    # seeded runs of the engine and of the oracle's restatement of the reference loop
+    # (reference precision) agree within their statistical error.  No exchanges, so every
+    # slot samples its own temperature; one energy per block after a burn-in block.
+    wl = workloads.make("c1")
+    sim = subset(wl, 8)
+    nseed, blocks, steps, burn = 16, 8, 250, 2
+
+    def acceptance(c):  # accepted / proposed over the run (no exchange resets the counters)
+        a = c["accept"].sum() + c["acceptA"].sum()
+        return a / max(1, a + c["reject"].sum())
+
+    def engine_means(seed):
+        w2 = workloads.Workload(wl.name, [sim], wl.lj_raw, wl.torsion_V, wl.torsion_phase, seed)
+        e = eng.from_workload(w2, cluster=1, threads=256)
+        samples = []
+        for b in range(blocks):
+            e.run(1, steps, exchange_after_last=False)
+            if b >= burn:
+                samples.append(e.replicas(0)["potential"].copy())
+        c = e.replicas(0)
+        e.close()
+        return np.mean(samples, 0), acceptance(c)
+
+    def oracle_means(seed):
+        o = OracleRemc(sim.molecules, wl.lj_raw, sim.box, sim.temperatures, sim.translate_steps, sim.rotate_steps,
+                       sim.move_weights, sim.rigid_rotate_prob, wl.torsion_V, wl.torsion_phase, seed=seed,
+                       mode=oracle.REF)
+        samples = []
+        for b in range(blocks):
+            o.run(1, steps, exchange_after_last=False, threads=8)
+            if b >= burn:
+                samples.append(o.potential.copy())
+        return np.mean(samples, 0), acceptance(o.counters())
+
+    e_runs = [engine_means(1000 + s) for s in range(nseed)]
+    o_runs = [oracle_means(2000 + s) for s in range(nseed)]
+    em, om = np.array([r[0] for r in e_runs]), np.array([r[0] for r in o_runs])
+    err = np.sqrt(em.var(0, ddof=1) / nseed + om.var(0, ddof=1) / nseed)
+    z = np.abs(em.mean(0) - om.mean(0)) / np.maximum(err, 1e-3)
+    assert np.all(z < 4.5), (em.mean(0), om.mean(0), err)
+    ea, oa = np.array([r[1] for r in e_runs]), np.array([r[1] for r in o_runs])
+    za = abs(ea.mean() - oa.mean()) / max(np.sqrt(ea.var(ddof=1) / nseed + oa.var(ddof=1) / nseed), 1e-4)
+    assert za < 4.5, (ea.mean(), oa.mean())
 
 
 def test_batched_simulations_match_separate_oracles():
