@@ -7,17 +7,21 @@
 // crowder).  The pair rules are those of the reference's flexible-linker build.
 //
 // Kernel: one CTA per (y-tile, x-tile) pair of 128-residue tiles on or above the
-// diagonal.  The x tile is copied in charged-first order, so the Debye-Hueckel term is
-// taken for charged x residues only; tile pairs that cannot hold an excluded pair
-// (checked per CTA from the key ranges of the two tiles) run that loop without exclusion
-// tests, the others with the tests per pair (the crowder forms keep a general loop).  The x tile is decoded once into shared memory (position and radius; the
-// exclusion keys of its w fields; charge, type and flags) next to the 20x20 table; two
-// threads own each y residue and sweep one half of the x tile each.  Pair terms are
-// FP32, summed per 32 pairs in two alternating partial sums and folded into
-// float-float accumulators, reduced per CTA in float-float.  The last CTA
-// to finish (ticket counter) reduces all CTA partials in a fixed order, so the total
-// is deterministic.  Scratch (partials + ticket + result) is per (device, stream),
-// allocated on first use and reused.
+// diagonal, two (one per 64-residue half of the y tile) for the diagonal pairs.  The x
+// tile is decoded once into shared memory (position and radius; the exclusion keys of
+// its w fields; charge, type and flags) next to the 20x20 table, and copied in the
+// order [charged | uncharged] real residues (padding left out), each part split into
+// the residues that cannot form an excluded pair with this CTA's y residues (their keys
+// outside the y residues' key ranges) and those that may: the Debye-Hueckel term is
+// taken for charged x residues only, and only the second kind takes the exclusion tests.
+// Per warp of y residues the tests are dropped altogether when none of its residues can
+// meet an excluded pair, or when the others share every x residue's domain (their sums
+// are discarded); the crowder forms keep a general loop where pairs may be excluded.
+// Two or four threads own each y residue and sweep alternate x residues.  Pair terms
+// are FP32, summed per 32 pairs and folded into float-float accumulators, reduced per
+// CTA in float-float.  The last CTA to finish (ticket counter) reduces all CTA partials
+// in a fixed order, so the total is deterministic.  Scratch (partials + ticket +
+// result) is per (device, stream), allocated on first use and reused.
 #include <cstdio>
 #include <atomic>
 #include <cstring>
@@ -96,29 +100,37 @@ struct PairCtx {
     bool ydom_nz, ybond_nz;
 };
 
-// The y residue against the x tile in charged-first order, the two threads of a y
-// residue taking alternate x residues: charged ones with the full term, then the rest
-// with the Lennard-Jones part alone (1/r^2 from the SFU reciprocal: no 1/r needed
-// there).  TESTED: the pairs the reference excludes (same rigid domain, same bond,
-// chain neighbours |x - y| < 4, padding, the diagonal tile's lower half) are evaluated
-// and selected away, with the rules of the general loop.
+// The y residue against a span of the copied x tile, the S threads of a y residue
+// taking every S-th x residue of the sequence j, j + S, ... below `end` (returns where
+// the sequence continues).  Charged spans take the full term, the others the
+// Lennard-Jones part alone (1/r^2 from the SFU reciprocal: no 1/r needed there).
+// TESTED spans hold the x residues that may form a pair the reference excludes (same
+// rigid domain, same bond, chain neighbours |x - y| < 4, the diagonal tile's lower
+// half), with the rules of the general loop: charged spans skip those pairs (a warp's y
+// residues mostly share a molecule, so the branch is mostly uniform), the others
+// evaluate them two at a time and select them away.
 template <bool TESTED>
-__device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const float4 *s_pq, const float2 *s_qt,
-                                                    const float4 *s_qk, int nqx, int half, FF &lj, FF &dh)
+__device__ __forceinline__ bool pair_excluded(const PairCtx &c, const float4 *s_qk, int j)
 {
-    auto excluded = [&](int j) -> bool {
-        if (!TESTED)
-            return false;
-        const float4 k = s_qk[j];
-        const int oi = __float_as_int(k.w), xi = oi & 0xffff;
-        return (oi >> 16) != 0 || (c.diag && xi <= c.yl) || (c.ydom_nz && k.x == c.ydom) ||
-               (c.ybond_nz && k.y == c.ybond) || (c.near && k.z == c.ychain && abs(c.x0 + xi - c.y) < 4);
-    };
+    if (!TESTED)
+        return false;
+    const float4 k = s_qk[j];
+    const int xi = __float_as_int(k.w);
+    return (c.diag && xi <= c.yl) || (c.ydom_nz && k.x == c.ydom) || (c.ybond_nz && k.y == c.ybond) ||
+           (c.near && k.z == c.ychain && abs(c.x0 + xi - c.y) < 4);
+}
+
+template <bool TESTED, int S>
+__device__ __forceinline__ int charged_span(const PairCtx &c, const float4 *s_pq, const float2 *s_qt,
+                                            const float4 *s_qk, int j, int end, FF &lj, FF &dh)
+{
     const float4 py = c.py;
     const float L = c.L, invL = c.invL;
-    float l0 = 0.f, l1 = 0.f, d0 = 0.f;
-    int j = half, cnt = 0;
-    for (; j < nqx; j += 2) {
+    float l0 = 0.f, d0 = 0.f;
+    int cnt = 0;
+    for (; j < end; j += S) {
+        if (pair_excluded<TESTED>(c, s_qk, j))
+            continue;
         const float4 px = s_pq[j];
         const float2 qt = s_qt[j];
         const float dx = min_image(py.x - px.x, L, invL);
@@ -128,9 +140,8 @@ __device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const floa
         const float inv_r = rsqrt_sfu(r2);
         const float u = lj_m4(c.m4row[__float_as_int(qt.y)], c.yh + px.w, inv_r * inv_r);
         const float d = dh_term(c.yq * qt.x, r2 * inv_r, inv_r);
-        const bool ex = excluded(j);
-        l0 += ex ? 0.f : u;
-        d0 += ex ? 0.f : d;
+        l0 += u;
+        d0 += d;
         if (++cnt == 32) {
             ff_add(lj, l0);
             ff_add(dh, d0);
@@ -140,42 +151,68 @@ __device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const floa
     }
     ff_add(lj, l0);
     ff_add(dh, d0);
-    l0 = 0.f;
-    cnt = 0;
-    for (; j + 2 < kTile; j += 4) {
-        const float4 pa = s_pq[j], pb = s_pq[j + 2];
-        const int ta = __float_as_int(s_qt[j].y), tb = __float_as_int(s_qt[j + 2].y);
+    return j;
+}
+
+template <bool TESTED, int S>
+__device__ __forceinline__ int lj_span(const PairCtx &c, const float4 *s_pq, const float2 *s_qt, const float4 *s_qk,
+                                       int j, int end, FF &lj)
+{
+    const float4 py = c.py;
+    const float L = c.L, invL = c.invL;
+    float l0 = 0.f, l1 = 0.f;
+    int cnt = 0;
+    for (; j + S < end; j += 2 * S) {
+        const float4 pa = s_pq[j], pb = s_pq[j + S];
+        const int ta = __float_as_int(s_qt[j].y), tb = __float_as_int(s_qt[j + S].y);
         const float ax = min_image(py.x - pa.x, L, invL), bx = min_image(py.x - pb.x, L, invL);
         const float ay = min_image(py.y - pa.y, L, invL), by = min_image(py.y - pb.y, L, invL);
         const float az = min_image(py.z - pa.z, L, invL), bz = min_image(py.z - pb.z, L, invL);
         const float ra = fmaf(ax, ax, fmaf(ay, ay, az * az)), rb = fmaf(bx, bx, fmaf(by, by, bz * bz));
         const float ua = lj_m4(c.m4row[ta], c.yh + pa.w, rcp_sfu(ra));
         const float ub = lj_m4(c.m4row[tb], c.yh + pb.w, rcp_sfu(rb));
-        l0 += excluded(j) ? 0.f : ua;
-        l1 += excluded(j + 2) ? 0.f : ub;
+        l0 += pair_excluded<TESTED>(c, s_qk, j) ? 0.f : ua;
+        l1 += pair_excluded<TESTED>(c, s_qk, j + S) ? 0.f : ub;
         if (++cnt == 16) {
             ff_add(lj, l0 + l1);
             l0 = l1 = 0.f;
             cnt = 0;
         }
     }
-    for (; j < kTile; j += 2) {
+    for (; j < end; j += S) {
         const float4 pa = s_pq[j];
         const float ax = min_image(py.x - pa.x, L, invL);
         const float ay = min_image(py.y - pa.y, L, invL);
         const float az = min_image(py.z - pa.z, L, invL);
         const float ra = fmaf(ax, ax, fmaf(ay, ay, az * az));
         const float ua = lj_m4(c.m4row[__float_as_int(s_qt[j].y)], c.yh + pa.w, rcp_sfu(ra));
-        l0 += excluded(j) ? 0.f : ua;
+        l0 += pair_excluded<TESTED>(c, s_qk, j) ? 0.f : ua;
     }
     ff_add(lj, l0 + l1);
+    return j;
 }
 
-// Folds one residue's exclusion keys into its tile's ranges (warp reductions, then one
-// shared atomic per warp and key) and flags.  Ranges are of the keys' bit patterns:
-// two sets of floats whose bit-pattern ranges are disjoint share no value.
-__device__ __forceinline__ void tile_keys(int *keys, int &tflags, float dom, float bond, float chain, float mol,
-                                          int flags, int t)
+// The y residue against the copied x tile: its real residues in the order [charged
+// safe | charged tested | uncharged safe | uncharged tested] with the group ends e[0..3]
+// (padding after e[3] is not visited); TESTED: the tested groups take the exclusion
+// tests (else the warp's y residues need none).
+template <int S, bool TESTED>
+__device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const float4 *s_pq, const float2 *s_qt,
+                                                    const float4 *s_qk, const int *e, int sub, FF &lj, FF &dh)
+{
+    int j = sub;
+    j = charged_span<false, S>(c, s_pq, s_qt, s_qk, j, e[0], lj, dh);
+    j = charged_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[1], lj, dh);
+    j = lj_span<false, S>(c, s_pq, s_qt, s_qk, j, e[2], lj);
+    lj_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[3], lj);
+}
+
+// One warp's residues' exclusion-key ranges and flags, stored by lane 0 into wk[0..10]:
+// [nonzero domain min/max, nonzero bond min/max, chain min/max, molecule min/max] as
+// bit patterns, the OR of the flags (bit 0 padding, bit 1 crowder), and the domain
+// min/max over every real residue (zero included).  Ranges are of the keys' bit
+// patterns: two sets of floats whose bit-pattern ranges are disjoint share no value.
+__device__ __forceinline__ void warp_keys(int *wk, float dom, float bond, float chain, float mol, int flags)
 {
     const int inf = 0x7fffffff;
     // + 0.0f turns -0 into +0: the exclusion tests compare keys as floats, where -0 == +0
@@ -185,25 +222,62 @@ __device__ __forceinline__ void tile_keys(int *keys, int &tflags, float dom, flo
     const int v[8] = {real && dom != 0.f ? d : inf, real && dom != 0.f ? d : -1,
                       real && bond != 0.f ? b : inf, real && bond != 0.f ? b : -1,
                       real ? c : inf, real ? c : -1, real && mol >= 0.f ? m : inf, real && mol >= 0.f ? m : -1};
-    const unsigned mask = __activemask();
+    int r[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int r = (k & 1) ? __reduce_max_sync(mask, v[k]) : __reduce_min_sync(mask, v[k]);
-        if ((t & 31) == 0) {
-            if (k & 1)
-                atomicMax(&keys[k], r);
-            else
-                atomicMin(&keys[k], r);
-        }
+    for (int k = 0; k < 8; ++k)
+        r[k] = (k & 1) ? __reduce_max_sync(0xffffffffu, v[k]) : __reduce_min_sync(0xffffffffu, v[k]);
+    const int f = (int)__reduce_or_sync(0xffffffffu, (unsigned)flags);
+    const int dlo = __reduce_min_sync(0xffffffffu, real ? d : inf), dhi = __reduce_max_sync(0xffffffffu, real ? d : -1);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            wk[k] = r[k];
+        wk[8] = f;
+        wk[9] = dlo;
+        wk[10] = dhi;
     }
-    const int f = (int)__reduce_or_sync(mask, (unsigned)flags);
-    if ((t & 31) == 0)
-        atomicOr(&tflags, f);
+}
+
+constexpr int kKeys = 11;
+
+// Key k of a tile from the nw warps that stored theirs (OR for the flags, k = 8; else
+// min for the lower bounds 0, 2, 4, 6, 9 and max for the upper ones).
+__device__ __forceinline__ int tile_key(const int (*wk)[kKeys], int nw, int k)
+{
+    const bool lower = (k < 8) ? (k & 1) == 0 : k == 9;
+    int v = wk[0][k];
+    for (int w = 1; w < nw; ++w)
+        v = (k == 8) ? (v | wk[w][k]) : lower ? min(v, wk[w][k]) : max(v, wk[w][k]);
+    return v;
 }
 
 __device__ __forceinline__ bool ranges_disjoint(int amin, int amax, int bmin, int bmax)
 {
     return amax < bmin || bmax < amin;  // an empty range (min > max) is disjoint from all
+}
+
+// CTAs of a call on nt tiles: every tile pair on or above the diagonal, the nt diagonal
+// pairs twice.
+__host__ __device__ inline int energy_ctas(int nt) { return nt * (nt + 1) / 2 + nt; }
+
+// CTA b -> tile pair (ty <= tx) and y part: part 1, 2 are the halves of the y tile of a
+// diagonal pair (CTAs 0 .. 2 nt - 1), part 0 the whole y tile of an off-diagonal pair
+// (row-major).
+__device__ __forceinline__ void cta_work(int b, int nt, int &ty, int &tx, int &part)
+{
+    if (b < 2 * nt) {
+        part = 1 + (b & 1);
+        ty = tx = b >> 1;
+        return;
+    }
+    part = 0;
+    int rem = b - 2 * nt;
+    ty = 0;
+    while (ty < nt - 1 && rem >= nt - ty - 1) {  // row ty holds nt - ty - 1 such pairs
+        rem -= nt - ty - 1;
+        ++ty;
+    }
+    tx = ty + 1 + rem;
 }
 
 // kNC: non-crowder pairs of different molecules only (E_TiledKernelNC).  kRC: the
@@ -231,22 +305,37 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     // ... and its exclusion keys (domain, bond, chain, original index | padding << 16) for
     // tile pairs that may hold excluded pairs (default potential)
     __shared__ float4 s_qk[kTile];
-    __shared__ unsigned s_qballot[kTile / 32];
-    // key ranges of the two tiles, [x, y][nonzero domain min/max, nonzero bond min/max,
-    // chain min/max, molecule min/max] as float bits, and [x, y] flags: bit 0 padding,
-    // bit 1 crowder
-    __shared__ int s_keys[2][8];
-    __shared__ int s_tflags[2];
+    // per-warp key ranges and flags of the x tile and of this CTA's y residues (warp_keys)
+    __shared__ int s_wk[2][kTile / 32][kKeys];
+    __shared__ int s_xr[kKeys];  // the x tile's keys (tile_key), for the y residues' classification
+    // counts of the x tile's copy groups per warp (charged safe, charged tested, uncharged
+    // safe, uncharged tested, padding)
+    __shared__ int s_gcnt[kTile / 32][5];
 
-    // Tile pair (ty <= tx) of this CTA, row-major over the upper triangle.
-    int rem = blockIdx.x, ty = 0;
-    while (rem >= nt - ty) {
-        rem -= nt - ty;
-        ++ty;
-    }
-    const int tx = ty + rem;
+    int ty, tx, part;
+    cta_work(blockIdx.x, nt, ty, tx, part);
     const int t = threadIdx.x;
-    const int yl = t & (kTile - 1), half = t / kTile;  // y residue, half of the x tile
+    // y residue of this thread (place in its tile) and its share of the x tile: the
+    // whole y tile with two threads per residue, or one half with four
+    const int ny = part ? kTile / 2 : kTile;
+    const int yl = (part ? (part - 1) * (kTile / 2) : 0) + (t & (ny - 1)), sub = t / ny;
+    // the x and y records first, so that their loads overlap the table's
+    const int x0 = tx * kTile;
+    const int y = ty * kTile + yl;
+    float4 px_in = make_float4(0.f, 0.f, 0.f, kPadder), mx_in = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (t < kTile && x0 + t < P) {
+        px_in = pos[x0 + t];
+        mx_in = meta[x0 + t];
+    }
+    const float4 py = (y < P) ? pos[y] : make_float4(0.f, 0.f, 0.f, kPadder);
+    const float4 my = (y < P) ? meta[y] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // the async form's output other than the total: zeroed by every CTA, a slice each
+    if (async_out != nullptr && async_count > 1) {
+        const int per = (async_count - 1 + (int)gridDim.x - 1) / (int)gridDim.x;
+        const int k0 = 1 + (int)blockIdx.x * per, k1 = min(async_count, k0 + per);
+        for (int k = k0 + t; k < k1; k += kThreads)
+            async_out[k] = 0.0f;
+    }
 
     for (int k = t; k < 400; k += kThreads)
     {
@@ -254,18 +343,13 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         s_eij[k] = e;
         s_m4[k] = -4.0f * e;
     }
-    if (t < 16)
-        s_keys[t >> 3][t & 7] = (t & 1) ? -1 : 0x7fffffff;  // empty ranges: min > max
-    if (t < 2)
-        s_tflags[t] = 0;
     __syncthreads();
     // residue types are checked once per residue (0..19; padding is excluded anyway):
     // the pair loop then indexes the table without a bounds test
     unsigned bad = 0;
-    const int x0 = tx * kTile;
+    unsigned qb = 0, rb = 0;  // this x warp's charged and real (not padding) residues
     if (t < kTile) {
-        const float4 px = (x0 + t < P) ? pos[x0 + t] : make_float4(0.f, 0.f, 0.f, kPadder);
-        const float4 mx = (x0 + t < P) ? meta[x0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 px = px_in, mx = mx_in;
         float xdom, xmol;
         const float xbond = frac_int(px.w, xdom);
         const float xchain = frac_int(mx.w, xmol);
@@ -282,58 +366,96 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         s_px[t] = make_float4(px.x, px.y, px.z, mx.z);
         s_xk[t] = make_float4(xdom, xbond, xchain, xmol);
         s_xm[t] = make_float4(mx.y, __int_as_float(xt), __int_as_float(xflags), 0.f);
-        tile_keys(s_keys[0], s_tflags[0], xdom, xbond, xchain, xmol, xflags, t);
-        const unsigned qb = __ballot_sync(0xffffffffu, mx.y != 0.0f);
-        if ((t & 31) == 0)
-            s_qballot[t >> 5] = qb;
+        warp_keys(s_wk[0][t >> 5], xdom, xbond, xchain, xmol, xflags);
+        qb = __ballot_sync(0xffffffffu, !pad && mx.y != 0.0f);
+        rb = __ballot_sync(0xffffffffu, !pad);
     }
-    const int y = ty * kTile + yl;
-    const float4 py = (y < P) ? pos[y] : make_float4(0.f, 0.f, 0.f, kPadder);
-    const float4 my = (y < P) ? meta[y] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (half == 0) {
+    if (sub == 0) {
         float ydom0, ymol0;
         const float ybond0 = frac_int(py.w, ydom0);
         const float ychain0 = frac_int(my.w, ymol0);
-        tile_keys(s_keys[1], s_tflags[1], ydom0, ybond0, ychain0, ymol0,
-                  (py.w == kPadder ? 1 : 0) | (my.w == kCrowder ? 2 : 0), t);
+        warp_keys(s_wk[1][t >> 5], ydom0, ybond0, ychain0, ymol0,
+                  (py.w == kPadder ? 1 : 0) | (my.w == kCrowder ? 2 : 0));
     }
     __syncthreads();
-    // No pair of the two tiles can be excluded when they are different tiles without
-    // padding (and, where crowders are treated apart, without crowders), their nonzero
-    // rigid-domain and bond keys share no value, and the chain rule (|x - y| < 4 on one
-    // chain) cannot apply (tiles two or more apart, or no common chain key); for the
-    // non-crowder sum also no common molecule.  Disjoint key ranges show the first ones.
-    bool clean = tx != ty && ((s_tflags[0] | s_tflags[1]) & ((kNC || kRC) ? 3 : 1)) == 0;
-    if (kNC)
-        clean = clean && ranges_disjoint(s_keys[0][6], s_keys[0][7], s_keys[1][6], s_keys[1][7]);
-    else
-        clean = clean && ranges_disjoint(s_keys[0][0], s_keys[0][1], s_keys[1][0], s_keys[1][1]) &&
-                ranges_disjoint(s_keys[0][2], s_keys[0][3], s_keys[1][2], s_keys[1][3]) &&
-                (tx - ty >= 2 || ranges_disjoint(s_keys[0][4], s_keys[0][5], s_keys[1][4], s_keys[1][5]));
-    // Other tile pairs of the default potential take the same charged-first loop with the
-    // exclusion tests per pair; the crowder forms keep the general loop.
-    const bool tested = !clean && !kNC && !kRC;
-    int nqx = 0;
-    if (clean || tested) {
-        // the x tile in charged-first order (stable): the Debye-Hueckel term is then taken
-        // for the charged x residues only
-        int before = 0;
-        for (int w = 0; w < kTile / 32; ++w)
-            nqx += __popc(s_qballot[w]);
+    const int nyw = ny / 32;  // warps that stored y keys
+    // No pair of the two tiles can be excluded when they are different tiles (where
+    // crowders are treated apart, without crowders), their nonzero rigid-domain and bond
+    // keys share no value, and the chain rule (|x - y| < 4 on one chain) cannot apply
+    // (tiles two or more apart, or no common chain key); for the non-crowder sum also no
+    // common molecule.  Disjoint key ranges show the first ones.  (Padding carries no
+    // keys and is left out of the charged-first copy.)
+    // (Only the crowder forms decide per tile pair; the default potential per x residue.)
+    bool clean = false;
+    if (kNC || kRC) {
+        auto kx = [&](int k) { return tile_key(s_wk[0], kTile / 32, k); };
+        auto ky = [&](int k) { return tile_key(s_wk[1], nyw, k); };
+        clean = tx != ty && ((kx(8) | ky(8)) & 2) == 0;
+        if (kNC)
+            clean = clean && ranges_disjoint(kx(6), kx(7), ky(6), ky(7));
+        else
+            clean = clean && ranges_disjoint(kx(0), kx(1), ky(0), ky(1)) && ranges_disjoint(kx(2), kx(3), ky(2), ky(3)) &&
+                    (tx - ty >= 2 || ranges_disjoint(kx(4), kx(5), ky(4), ky(5)));
+    }
+    // The default potential always takes the charged-first loop: each x residue that may
+    // form an excluded pair with this CTA's y residues (a diagonal tile; its nonzero domain
+    // or bond key inside the y residues' ranges; its chain key inside theirs where the
+    // chain rule can apply) is tested per pair, the others are not.  The crowder forms
+    // take it for clean tile pairs only, the general loop otherwise.
+    const bool cfirst = clean || (!kNC && !kRC);
+    int e[4] = {0, 0, 0, 0};  // ends of the copy's groups (see charged_first_pairs)
+    if (cfirst) {
+        // the x tile's real residues in the order [charged safe | charged tested | uncharged
+        // safe | uncharged tested] (stable within each group), padding after them: the
+        // Debye-Hueckel term is then taken for the charged x residues only
+        unsigned gm[5] = {0u, 0u, 0u, 0u, 0u};  // this x warp's residues by group
         if (t < kTile) {
-            const unsigned qb = s_qballot[t >> 5];
-            const unsigned below = qb & ((1u << (t & 31)) - 1u);
-            for (int w = 0; w < (t >> 5); ++w)
-                before += __popc(s_qballot[w]);
-            const bool q = (qb >> (t & 31)) & 1u;
-            const int k = q ? before + __popc(below) : nqx + (t - before - __popc(below));
+            bool u = false;
+            if (!kNC && !kRC) {
+                const float4 xk = s_xk[t];
+                const int d = __float_as_int(xk.x + 0.0f), b = __float_as_int(xk.y + 0.0f),
+                          ch = __float_as_int(xk.z + 0.0f);
+                u = tx == ty || (xk.x != 0.f && tile_key(s_wk[1], nyw, 0) <= d && d <= tile_key(s_wk[1], nyw, 1)) ||
+                    (xk.y != 0.f && tile_key(s_wk[1], nyw, 2) <= b && b <= tile_key(s_wk[1], nyw, 3)) ||
+                    (tx - ty <= 1 && tile_key(s_wk[1], nyw, 4) <= ch && ch <= tile_key(s_wk[1], nyw, 5));
+            }
+            const unsigned ub = __ballot_sync(0xffffffffu, u);
+            gm[0] = qb & ~ub;
+            gm[1] = qb & ub;
+            gm[2] = rb & ~qb & ~ub;
+            gm[3] = rb & ~qb & ub;
+            gm[4] = ~rb;
+            if ((t & 31) == 0)
+#pragma unroll
+                for (int g = 0; g < 5; ++g)
+                    s_gcnt[t >> 5][g] = __popc(gm[g]);
+        } else if (t < kTile + kKeys) {
+            s_xr[t - kTile] = tile_key(s_wk[0], kTile / 32, t - kTile);
+        }
+        __syncthreads();
+        int acc = 0;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            for (int w = 0; w < kTile / 32; ++w)
+                acc += s_gcnt[w][g];
+            e[g] = acc;
+        }
+        if (t < kTile) {
+            // this residue's group g, its members in this warp (mg) and the group's start
+            const int w0 = t >> 5;
+            const unsigned me = 1u << (t & 31);
+            const int g = (gm[0] & me) ? 0 : (gm[1] & me) ? 1 : (gm[2] & me) ? 2 : (gm[3] & me) ? 3 : 4;
+            const unsigned mg = g == 0 ? gm[0] : g == 1 ? gm[1] : g == 2 ? gm[2] : g == 3 ? gm[3] : gm[4];
+            int k = (g == 0 ? 0 : g == 1 ? e[0] : g == 2 ? e[1] : g == 3 ? e[2] : e[3]) + __popc(mg & (me - 1u));
+            for (int w = 0; w < w0; ++w)
+                k += s_gcnt[w][g];
             const float4 xm = s_xm[t];
             float4 pw = s_px[t];
             pw.w *= 0.5f;  // half the radius: sigma_ij = half_y + half_x
             s_pq[k] = pw;
             s_qt[k] = make_float2(xm.x, xm.y);
             const float4 xk = s_xk[t];
-            s_qk[k] = make_float4(xk.x, xk.y, xk.z, __int_as_float(t | ((__float_as_int(xm.z) & 1) << 16)));
+            s_qk[k] = make_float4(xk.x, xk.y, xk.z, __int_as_float(t));
         }
         __syncthreads();
     }
@@ -341,6 +463,25 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     FF lj{0.f, 0.f}, dh{0.f, 0.f};
     const bool ycrowd = my.w == kCrowder;
     const bool active = (py.w > kPadder) && (!kNC || !ycrowd);
+    // Default potential, per warp of y residues: a y residue is x-safe when none of its
+    // keys can meet the x tile's (an off-diagonal tile; its nonzero domain and bond keys
+    // outside the tile's ranges; its chain key too where the chain rule can apply), and
+    // all-excluded when every real x residue shares its nonzero domain.  A warp with
+    // neither kind needing the tests runs the loop untested (all-excluded lanes discard
+    // their sums), one with only all-excluded lanes skips it, the others test per pair.
+    bool allex = false, wskip = false, wtested = true;
+    if (!kNC && !kRC && cfirst) {
+        float yd0, ym0;
+        const float yb0 = frac_int(py.w, yd0);
+        const float yc0 = frac_int(my.w, ym0);
+        const int yd = __float_as_int(yd0 + 0.0f), yb = __float_as_int(yb0 + 0.0f), yc = __float_as_int(yc0 + 0.0f);
+        const bool xsafe = tx != ty && !(yd0 != 0.f && s_xr[0] <= yd && yd <= s_xr[1]) &&
+                           !(yb0 != 0.f && s_xr[2] <= yb && yb <= s_xr[3]) &&
+                           !(tx - ty <= 1 && s_xr[4] <= yc && yc <= s_xr[5]);
+        allex = yd0 != 0.f && s_xr[9] == yd && s_xr[10] == yd;
+        wskip = !__any_sync(0xffffffffu, active && !allex);
+        wtested = __any_sync(0xffffffffu, active && !xsafe && !allex);
+    }
     if (active) {
         const float L = c_boxdim;
         const float invL = (L != 0.0f) ? 1.0f / L : 0.0f;
@@ -358,16 +499,26 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         }
         const float *erow = s_eij + 20 * yt;
         const float yq = my.y, ys = my.z;
-        if (clean || tested) {
+        if (cfirst && !wskip) {
             const PairCtx c{py, 0.5f * ys, yq, s_m4 + 20 * yt, L, invL, yl, x0, y, diag, near, ydom, ybond, ychain,
                             ydom_nz, ybond_nz};
-            if (clean)
-                charged_first_pairs<false>(c, s_pq, s_qt, s_qk, nqx, half, lj, dh);
-            else
-                charged_first_pairs<true>(c, s_pq, s_qt, s_qk, nqx, half, lj, dh);
+            if (wtested) {
+                if (part == 0)
+                    charged_first_pairs<2, true>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+                else
+                    charged_first_pairs<4, true>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+            } else {
+                if (part == 0)
+                    charged_first_pairs<2, false>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+                else
+                    charged_first_pairs<4, false>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+                if (allex)  // every pair of this y residue is excluded
+                    lj = dh = FF{0.f, 0.f};
+            }
         }
-        const int jb0 = half * (kTile / 2);
-        for (int jb = jb0; !clean && !tested && jb < jb0 + kTile / 2; jb += 32) {
+        // the general loop: this thread's share of the x tile, kTile / S consecutive residues
+        const int jw = part ? kTile / 4 : kTile / 2, jb0 = sub * jw;
+        for (int jb = jb0; !cfirst && jb < jb0 + jw; jb += 32) {
             float l0 = 0.f, l1 = 0.f, d0 = 0.f, d1 = 0.f;
             // branch-free: every pair is evaluated and the excluded ones (padding, the
             // pair itself on the diagonal: possibly inf / NaN) are selected away
@@ -473,9 +624,6 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
             async_out[0] = (float)total;
         *ticket = 0u;
     }
-    if (async_out != nullptr)
-        for (int k = 1 + t; k < async_count; k += kThreads)
-            async_out[k] = 0.0f;
 }
 
 int current_device()
@@ -515,11 +663,14 @@ const float *bound_table()
 }
 
 // Launch the tile kernel on `stream`.  Returns 0 on success.
+// Launch the tile kernel on `stream`.  Returns 0 on success.  (A programmatic dependent
+// launch, scheduled during the previous call's last CTAs, measured slower: the new CTAs
+// land on the SMs that happen to be free and pile up to five per SM on half of them.)
 int launch_energy(bool nc, const float4 *pos, const float4 *meta, int P, const float *table, Scratch *s,
                   float *async_out, int async_count, cudaStream_t stream)
 {
     const int nt = (P + kTile - 1) / kTile;
-    const int blocks = nt * (nt + 1) / 2;
+    const int blocks = energy_ctas(nt);
     // crowders take no part in the non-crowder sum, so its form has no crowder variant
     const bool rc = g_repulsive_crowding.load() != 0;
     if (nc)
@@ -547,7 +698,7 @@ void eon_device_sync(bool nc, float4 *pos, float4 *meta, double *result, int dat
         return;
     }
     const int nt = (datasetSize + kTile - 1) / kTile;
-    Scratch *s = scratch_for(cudaStreamLegacy, (size_t)nt * (nt + 1) / 2);
+    Scratch *s = scratch_for(cudaStreamLegacy, (size_t)energy_ctas(nt));
     if (s == nullptr)
         return;
     if (launch_energy(nc, pos, meta, datasetSize, table, s, nullptr, 0, cudaStreamLegacy) != 0)
@@ -664,7 +815,7 @@ void CUDA_EonDevice_async(float4 *residuePositions, float4 *residueMeta, int *re
         return;
     }
     const int nt = (datasetSize + kTile - 1) / kTile;
-    Scratch *s = scratch_for(stream, (size_t)nt * (nt + 1) / 2);
+    Scratch *s = scratch_for(stream, (size_t)energy_ctas(nt));
     if (s == nullptr)
         return;
     launch_energy(false, residuePositions, residueMeta, datasetSize, table, s, device_result,
@@ -708,9 +859,9 @@ namespace {
 
 constexpr int kNoAllocMaxResidues = 16384;                       // datasetSize limit
 constexpr int kNoAllocMaxTiles = kNoAllocMaxResidues / kTile;    // 128-residue tiles
-constexpr int kNoAllocMaxCtas = kNoAllocMaxTiles * (kNoAllocMaxTiles + 1) / 2;
+constexpr int kNoAllocMaxCtas = kNoAllocMaxTiles * (kNoAllocMaxTiles + 1) / 2 + 2 * kNoAllocMaxTiles - 1;
 // layout: [0] ticket, [4] flags, [256] result (3 doubles), [512] 16 bytes per CTA
-constexpr size_t kNoAllocBytes = 512 + 2 * sizeof(double) * kNoAllocMaxCtas;  // 132,608 bytes
+constexpr size_t kNoAllocBytes = 512 + 2 * sizeof(double) * kNoAllocMaxCtas;  // 136,688 bytes
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
