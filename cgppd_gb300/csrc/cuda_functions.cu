@@ -49,13 +49,38 @@ __constant__ float c_boxdim;  // CUDA_setBoxDimension, module state per device
 // (src/definitions.h:18) as process-wide module state, read at each launch
 std::atomic<int> g_repulsive_crowding{0};
 
+// CTAs are reduced in groups of kGroup: the last CTA of a group to finish sums the
+// group's partials, the last group to finish sums the group sums.
+constexpr int kGroup = 32;
+
 struct Scratch {
-    unsigned *ticket = nullptr;   // CTA completion counter, self-resetting
+    unsigned *ticket = nullptr;   // group completion counter, self-resetting
     unsigned *flags = nullptr;    // bit 0: residue type index out of range
     double *result = nullptr;     // {LJ raw, DH raw, total kcal/mol}
     double *partials = nullptr;   // 16 bytes per CTA: its LJ and DH sums as float-float
+    float4 *gsums = nullptr;      // 16 bytes per group: its LJ and DH sums as float-float
+    unsigned *gtickets = nullptr; // CTA completion counter per group, self-resetting
     size_t capacity = 0;          // CTAs the partials can hold
 };
+
+// Scratch layout for `cap` CTAs: [ticket, flags | pad to 256] [result: 4 doubles | pad]
+// [partials: 16 bytes per CTA] [group sums: 16 bytes per group] [group tickets: 4 bytes
+// per group]; the counters (the first 8 bytes and the group tickets) start at zero.
+constexpr size_t scratch_groups(size_t cap) { return (cap + kGroup - 1) / kGroup; }
+constexpr size_t scratch_gsums_at(size_t cap) { return 512 + 16 * cap; }
+constexpr size_t scratch_gtickets_at(size_t cap) { return scratch_gsums_at(cap) + 16 * scratch_groups(cap); }
+constexpr size_t scratch_bytes(size_t cap) { return scratch_gtickets_at(cap) + 4 * scratch_groups(cap); }
+
+void scratch_view(unsigned char *base, size_t cap, Scratch &s)
+{
+    s.ticket = reinterpret_cast<unsigned *>(base);
+    s.flags = reinterpret_cast<unsigned *>(base + 4);
+    s.result = reinterpret_cast<double *>(base + 256);
+    s.partials = reinterpret_cast<double *>(base + 512);
+    s.gsums = reinterpret_cast<float4 *>(base + scratch_gsums_at(cap));
+    s.gtickets = reinterpret_cast<unsigned *>(base + scratch_gtickets_at(cap));
+    s.capacity = cap;
+}
 
 std::mutex g_mu;
 std::map<std::pair<int, cudaStream_t>, Scratch> g_scratch;
@@ -195,16 +220,20 @@ __device__ __forceinline__ int lj_span(const PairCtx &c, const float4 *s_pq, con
 // The y residue against the copied x tile: its real residues in the order [charged
 // safe | charged tested | uncharged safe | uncharged tested] with the group ends e[0..3]
 // (padding after e[3] is not visited); TESTED: the tested groups take the exclusion
-// tests (else the warp's y residues need none).
+// tests (else the warp's y residues need none, and skip_tested residues skip them).
 template <int S, bool TESTED>
 __device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const float4 *s_pq, const float2 *s_qt,
-                                                    const float4 *s_qk, const int *e, int sub, FF &lj, FF &dh)
+                                                    const float4 *s_qk, const int *e, int sub, bool skip_tested,
+                                                    FF &lj, FF &dh)
 {
+    // the first index of the sequence j, j + S, ... at or past `end`
+    auto past = [](int j, int end) { return j < end ? j + ((end - j + S - 1) / S) * S : j; };
     int j = sub;
     j = charged_span<false, S>(c, s_pq, s_qt, s_qk, j, e[0], lj, dh);
-    j = charged_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[1], lj, dh);
+    j = skip_tested ? past(j, e[1]) : charged_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[1], lj, dh);
     j = lj_span<false, S>(c, s_pq, s_qt, s_qk, j, e[2], lj);
-    lj_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[3], lj);
+    if (!skip_tested)
+        lj_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[3], lj);
 }
 
 // One warp's residues' exclusion-key ranges and flags, stored by lane 0 into wk[0..10]:
@@ -258,7 +287,7 @@ __device__ __forceinline__ bool ranges_disjoint(int amin, int amax, int bmin, in
 
 // CTAs of a call on nt tiles: every tile pair on or above the diagonal, the nt diagonal
 // pairs twice.
-__host__ __device__ inline int energy_ctas(int nt) { return nt * (nt + 1) / 2 + nt; }
+__host__ __device__ constexpr int energy_ctas(int nt) { return nt * (nt + 1) / 2 + nt; }
 
 // CTA b -> tile pair (ty <= tx) and y part: part 1, 2 are the halves of the y tile of a
 // diagonal pair (CTAs 0 .. 2 nt - 1), part 0 the whole y tile of an off-diagonal pair
@@ -287,6 +316,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
                                                           int P, int nt, const float *__restrict__ lj_raw,
                                                           double *__restrict__ partials, unsigned *__restrict__ ticket,
                                                           unsigned *__restrict__ flags, double *__restrict__ result,
+                                                          float4 *__restrict__ gsums, unsigned *__restrict__ gtickets,
                                                           float *__restrict__ async_out, int async_count)
 {
     // x tile, decoded once per CTA: position and vdW radius; exclusion keys (rigid
@@ -297,7 +327,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     __shared__ float s_eij[400];
     __shared__ float s_m4[400];   // -4 Eij in RT units (the clean-tile loop's form)
     __shared__ FF s_red[2][kWarps];
-    __shared__ bool s_last;
+    __shared__ bool s_last, s_last_group;
     // the x tile again in charged-first order (position + radius, charge + type) for
     // tile pairs without any excluded pair
     __shared__ float4 s_pq[kTile];
@@ -307,11 +337,16 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     __shared__ float4 s_qk[kTile];
     // per-warp key ranges and flags of the x tile and of this CTA's y residues (warp_keys)
     __shared__ int s_wk[2][kTile / 32][kKeys];
-    __shared__ int s_xr[kKeys];  // the x tile's keys (tile_key), for the y residues' classification
+    // per x warp, key ranges of its residues that take the exclusion tests: [nonzero domain
+    // min/max, nonzero bond min/max, chain min/max, domain min/max] (bit patterns)
+    __shared__ int s_tk[kTile / 32][8];
     // counts of the x tile's copy groups per warp (charged safe, charged tested, uncharged
     // safe, uncharged tested, padding)
     __shared__ int s_gcnt[kTile / 32][5];
 
+    // a dependent launch (see launch_energy): nothing global is touched before the
+    // stream's previous kernel has completed
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     int ty, tx, part;
     cta_work(blockIdx.x, nt, ty, tx, part);
     const int t = threadIdx.x;
@@ -420,6 +455,24 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
                     (tx - ty <= 1 && tile_key(s_wk[1], nyw, 4) <= ch && ch <= tile_key(s_wk[1], nyw, 5));
             }
             const unsigned ub = __ballot_sync(0xffffffffu, u);
+            {
+                const float4 xk = s_xk[t];
+                const bool tst = u && ((rb >> (t & 31)) & 1u);
+                const int inf = 0x7fffffff;
+                const int d = __float_as_int(xk.x + 0.0f), b = __float_as_int(xk.y + 0.0f),
+                          ch = __float_as_int(xk.z + 0.0f);
+                const int v[8] = {tst && xk.x != 0.f ? d : inf, tst && xk.x != 0.f ? d : -1,
+                                  tst && xk.y != 0.f ? b : inf, tst && xk.y != 0.f ? b : -1,
+                                  tst ? ch : inf, tst ? ch : -1, tst ? d : inf, tst ? d : -1};
+                int r[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    r[k] = (k & 1) ? __reduce_max_sync(0xffffffffu, v[k]) : __reduce_min_sync(0xffffffffu, v[k]);
+                if ((t & 31) == 0)
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        s_tk[t >> 5][k] = r[k];
+            }
             gm[0] = qb & ~ub;
             gm[1] = qb & ub;
             gm[2] = rb & ~qb & ~ub;
@@ -429,8 +482,6 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
 #pragma unroll
                 for (int g = 0; g < 5; ++g)
                     s_gcnt[t >> 5][g] = __popc(gm[g]);
-        } else if (t < kTile + kKeys) {
-            s_xr[t - kTile] = tile_key(s_wk[0], kTile / 32, t - kTile);
         }
         __syncthreads();
         int acc = 0;
@@ -463,24 +514,34 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     FF lj{0.f, 0.f}, dh{0.f, 0.f};
     const bool ycrowd = my.w == kCrowder;
     const bool active = (py.w > kPadder) && (!kNC || !ycrowd);
-    // Default potential, per warp of y residues: a y residue is x-safe when none of its
-    // keys can meet the x tile's (an off-diagonal tile; its nonzero domain and bond keys
-    // outside the tile's ranges; its chain key too where the chain rule can apply), and
-    // all-excluded when every real x residue shares its nonzero domain.  A warp with
-    // neither kind needing the tests runs the loop untested (all-excluded lanes discard
-    // their sums), one with only all-excluded lanes skips it, the others test per pair.
-    bool allex = false, wskip = false, wtested = true;
+    // Default potential, per y residue against the tested x residues (keys s_tk): it is
+    // safe when none of its keys can meet theirs (an off-diagonal tile; its nonzero domain
+    // and bond keys outside their ranges; its chain key too where the chain rule can
+    // apply), and all-excluded when they all share its nonzero domain.  A warp whose y
+    // residues are all one or the other takes the tested groups without tests (the
+    // all-excluded residues skip them); otherwise it tests per pair.
+    bool skip_tested = false, wtested = true;
     if (!kNC && !kRC && cfirst) {
+        // the tested residues' key k: lane k combines the x warps' values, then a broadcast
+        int tk = 0;
+        if ((t & 31) < 8) {
+            const int k = t & 31;
+            tk = s_tk[0][k];
+            for (int w = 1; w < kTile / 32; ++w)
+                tk = (k & 1) ? max(tk, s_tk[w][k]) : min(tk, s_tk[w][k]);
+        }
+        int T[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            T[k] = __shfl_sync(0xffffffffu, tk, k);
         float yd0, ym0;
         const float yb0 = frac_int(py.w, yd0);
         const float yc0 = frac_int(my.w, ym0);
         const int yd = __float_as_int(yd0 + 0.0f), yb = __float_as_int(yb0 + 0.0f), yc = __float_as_int(yc0 + 0.0f);
-        const bool xsafe = tx != ty && !(yd0 != 0.f && s_xr[0] <= yd && yd <= s_xr[1]) &&
-                           !(yb0 != 0.f && s_xr[2] <= yb && yb <= s_xr[3]) &&
-                           !(tx - ty <= 1 && s_xr[4] <= yc && yc <= s_xr[5]);
-        allex = yd0 != 0.f && s_xr[9] == yd && s_xr[10] == yd;
-        wskip = !__any_sync(0xffffffffu, active && !allex);
-        wtested = __any_sync(0xffffffffu, active && !xsafe && !allex);
+        const bool lsafe = tx != ty && !(yd0 != 0.f && T[0] <= yd && yd <= T[1]) &&
+                           !(yb0 != 0.f && T[2] <= yb && yb <= T[3]) && !(tx - ty <= 1 && T[4] <= yc && yc <= T[5]);
+        skip_tested = yd0 != 0.f && T[6] == yd && T[7] == yd;
+        wtested = __any_sync(0xffffffffu, active && !lsafe && !skip_tested);
     }
     if (active) {
         const float L = c_boxdim;
@@ -499,21 +560,19 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         }
         const float *erow = s_eij + 20 * yt;
         const float yq = my.y, ys = my.z;
-        if (cfirst && !wskip) {
+        if (cfirst) {
             const PairCtx c{py, 0.5f * ys, yq, s_m4 + 20 * yt, L, invL, yl, x0, y, diag, near, ydom, ybond, ychain,
                             ydom_nz, ybond_nz};
             if (wtested) {
                 if (part == 0)
-                    charged_first_pairs<2, true>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+                    charged_first_pairs<2, true>(c, s_pq, s_qt, s_qk, e, sub, false, lj, dh);
                 else
-                    charged_first_pairs<4, true>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+                    charged_first_pairs<4, true>(c, s_pq, s_qt, s_qk, e, sub, false, lj, dh);
             } else {
                 if (part == 0)
-                    charged_first_pairs<2, false>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
+                    charged_first_pairs<2, false>(c, s_pq, s_qt, s_qk, e, sub, skip_tested, lj, dh);
                 else
-                    charged_first_pairs<4, false>(c, s_pq, s_qt, s_qk, e, sub, lj, dh);
-                if (allex)  // every pair of this y residue is excluded
-                    lj = dh = FF{0.f, 0.f};
+                    charged_first_pairs<4, false>(c, s_pq, s_qt, s_qk, e, sub, skip_tested, lj, dh);
             }
         }
         // the general loop: this thread's share of the x tile, kTile / S consecutive residues
@@ -565,6 +624,9 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         }
     }
 
+    // the stream's next call may be scheduled once every CTA is past its pair work: its
+    // CTAs then spread over SMs that are mostly idle, and wait for this kernel to end
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // CTA reduction in float-float on the FP32 pipe (the FP64 unit is slow on this part).
     // Each CTA leaves (LJ hi, LJ lo, DH hi, DH lo) in its 16-byte partials slot.
     float4 *part4 = reinterpret_cast<float4 *>(partials);
@@ -586,43 +648,60 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
         }
         part4[blockIdx.x] = make_float4(a.hi, a.lo, b.hi, b.lo);
         __threadfence();
-        const unsigned done = atomicAdd(ticket, 1u);
-        s_last = (done == gridDim.x - 1);
+        const int g = blockIdx.x / kGroup, gsize = min(kGroup, (int)gridDim.x - g * kGroup);
+        const unsigned done = atomicAdd(&gtickets[g], 1u);
+        s_last = (done == (unsigned)gsize - 1u);
     }
     __syncthreads();
     if (!s_last)
         return;
 
-    // Last CTA: every CTA's partials in a fixed order, float-float, then FP64 once.
+    // Last CTA of its group: the group's partials in a fixed order (float-float, one warp).
     __threadfence();
-    FF a{0.f, 0.f}, b{0.f, 0.f};
-    for (int k = t; k < (int)gridDim.x; k += kThreads) {
-        const float4 p = __ldcg(&part4[k]);
-        ff_add_ff(a, FF{p.x, p.y});
-        ff_add_ff(b, FF{p.z, p.w});
-    }
-    a = ff_warp_sum(a);
-    b = ff_warp_sum(b);
-    __syncthreads();
-    if ((t & 31) == 0) {
-        s_red[0][t >> 5] = a;
-        s_red[1][t >> 5] = b;
-    }
-    __syncthreads();
-    if (t == 0) {
-        FF A = s_red[0][0], B = s_red[1][0];
-        for (int w = 1; w < kWarps; ++w) {
-            ff_add_ff(A, s_red[0][w]);
-            ff_add_ff(B, s_red[1][w]);
+    const int ngroups = ((int)gridDim.x + kGroup - 1) / kGroup;
+    if (t < 32) {
+        const int g = blockIdx.x / kGroup, c0 = g * kGroup, gsize = min(kGroup, (int)gridDim.x - c0);
+        FF a{0.f, 0.f}, b{0.f, 0.f};
+        if (t < gsize) {
+            const float4 p = __ldcg(&part4[c0 + t]);
+            a = FF{p.x, p.y};
+            b = FF{p.z, p.w};
         }
-        const double lj_raw_sum = ff_value(A), dh_raw_sum = ff_value(B);
-        const double total = lj_raw_sum * (double)kRTtoKcal + dh_raw_sum * (double)kDHFactor;
-        result[0] = lj_raw_sum;
-        result[1] = dh_raw_sum;
-        result[2] = total;
-        if (async_out != nullptr && async_count > 0)
-            async_out[0] = (float)total;
-        *ticket = 0u;
+        a = ff_warp_sum(a);
+        b = ff_warp_sum(b);
+        if (t == 0) {
+            gsums[g] = make_float4(a.hi, a.lo, b.hi, b.lo);
+            gtickets[g] = 0u;
+            __threadfence();
+            const unsigned done = atomicAdd(ticket, 1u);
+            s_last_group = (done == (unsigned)ngroups - 1u);
+        }
+    }
+    __syncthreads();
+    if (!s_last_group)
+        return;
+
+    // Last group: every group's sum in a fixed order, float-float, then FP64 once.
+    __threadfence();
+    if (t < 32) {
+        FF a{0.f, 0.f}, b{0.f, 0.f};
+        for (int g = t; g < ngroups; g += 32) {
+            const float4 p = __ldcg(&gsums[g]);
+            ff_add_ff(a, FF{p.x, p.y});
+            ff_add_ff(b, FF{p.z, p.w});
+        }
+        a = ff_warp_sum(a);
+        b = ff_warp_sum(b);
+        if (t == 0) {
+            const double lj_raw_sum = ff_value(a), dh_raw_sum = ff_value(b);
+            const double total = lj_raw_sum * (double)kRTtoKcal + dh_raw_sum * (double)kDHFactor;
+            result[0] = lj_raw_sum;
+            result[1] = dh_raw_sum;
+            result[2] = total;
+            if (async_out != nullptr && async_count > 0)
+                async_out[0] = (float)total;
+            *ticket = 0u;
+        }
     }
 }
 
@@ -641,17 +720,11 @@ Scratch *scratch_for(cudaStream_t stream, size_t blocks)
         if (s.ticket != nullptr)
             cudaFree(s.ticket);
         size_t cap = blocks < 256 ? 256 : blocks;
-        char *base = nullptr;
-        // [ticket, flags | pad to 256] [result: 4 doubles | pad] [partials]
-        size_t bytes = 256 + 256 + 2 * sizeof(double) * cap;
-        if (cgppd_check(cudaMalloc(&base, bytes), "scratch allocation") != 0)
+        unsigned char *base = nullptr;
+        if (cgppd_check(cudaMalloc(&base, scratch_bytes(cap)), "scratch allocation") != 0)
             return nullptr;
-        cudaMemset(base, 0, 512);
-        s.ticket = reinterpret_cast<unsigned *>(base);
-        s.flags = reinterpret_cast<unsigned *>(base + 4);
-        s.result = reinterpret_cast<double *>(base + 256);
-        s.partials = reinterpret_cast<double *>(base + 512);
-        s.capacity = cap;
+        cudaMemset(base, 0, scratch_bytes(cap));
+        scratch_view(base, cap, s);
     }
     return &s;
 }
@@ -663,26 +736,33 @@ const float *bound_table()
 }
 
 // Launch the tile kernel on `stream`.  Returns 0 on success.
-// Launch the tile kernel on `stream`.  Returns 0 on success.  (A programmatic dependent
-// launch, scheduled during the previous call's last CTAs, measured slower: the new CTAs
-// land on the SMs that happen to be free and pile up to five per SM on half of them.)
+// Launch the tile kernel on `stream`.  Returns 0 on success.  On a stream of the caller
+// (the asynchronous entry point) the launch is a programmatic dependent one: the grid
+// may be scheduled once every CTA of the stream's previous kernel has finished its pair
+// work (for a previous call of this kernel), and each CTA waits for that kernel's
+// completion (griddepcontrol.wait) before it reads or writes global memory, so the
+// ordering the caller sees is that of a plain launch.
 int launch_energy(bool nc, const float4 *pos, const float4 *meta, int P, const float *table, Scratch *s,
                   float *async_out, int async_count, cudaStream_t stream)
 {
     const int nt = (P + kTile - 1) / kTile;
-    const int blocks = energy_ctas(nt);
     // crowders take no part in the non-crowder sum, so its form has no crowder variant
     const bool rc = g_repulsive_crowding.load() != 0;
-    if (nc)
-        k_tile_energy<true, false><<<blocks, kThreads, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket,
-                                                                    s->flags, s->result, async_out, async_count);
-    else if (rc)
-        k_tile_energy<false, true><<<blocks, kThreads, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket,
-                                                                    s->flags, s->result, async_out, async_count);
-    else
-        k_tile_energy<false, false><<<blocks, kThreads, 0, stream>>>(pos, meta, P, nt, table, s->partials, s->ticket,
-                                                                     s->flags, s->result, async_out, async_count);
-    return cgppd_check(cudaGetLastError(), "energy kernel launch");
+    auto kern = nc ? k_tile_energy<true, false> : rc ? k_tile_energy<false, true> : k_tile_energy<false, false>;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)energy_ctas(nt));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    const bool dependent = stream != cudaStreamLegacy && stream != nullptr;
+    cfg.attrs = dependent ? attr : nullptr;
+    cfg.numAttrs = dependent ? 1 : 0;
+    return cgppd_check(cudaLaunchKernelEx(&cfg, kern, pos, meta, P, nt, table, s->partials, s->ticket, s->flags,
+                                          s->result, s->gsums, s->gtickets, async_out, async_count),
+                       "energy kernel launch");
 }
 
 // Synchronous total on the legacy default stream (the reference's stream 0).
@@ -859,9 +939,9 @@ namespace {
 
 constexpr int kNoAllocMaxResidues = 16384;                       // datasetSize limit
 constexpr int kNoAllocMaxTiles = kNoAllocMaxResidues / kTile;    // 128-residue tiles
-constexpr int kNoAllocMaxCtas = kNoAllocMaxTiles * (kNoAllocMaxTiles + 1) / 2 + 2 * kNoAllocMaxTiles - 1;
-// layout: [0] ticket, [4] flags, [256] result (3 doubles), [512] 16 bytes per CTA
-constexpr size_t kNoAllocBytes = 512 + 2 * sizeof(double) * kNoAllocMaxCtas;  // 136,688 bytes
+constexpr int kNoAllocMaxCtas = energy_ctas(kNoAllocMaxTiles);
+constexpr size_t kNoAllocBytes = scratch_bytes(kNoAllocMaxCtas);  // 139,896 bytes (layout: scratch_view)
+static_assert(kNoAllocBytes == 139896, "the documented size of the static scratch");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -927,12 +1007,10 @@ void CUDA_EonDevice_noalloc(float4 *residuePositions, float4 *residueMeta, int *
     if (base == nullptr)
         return;
     Scratch s;
-    s.ticket = reinterpret_cast<unsigned *>(base);
-    s.flags = reinterpret_cast<unsigned *>(base + 4);
-    s.result = reinterpret_cast<double *>(base + 256);
-    s.partials = reinterpret_cast<double *>(base + 512);
-    s.capacity = kNoAllocMaxCtas;
-    if (cgppd_check(cudaMemsetAsync(base, 0, 8, cudaStreamLegacy), "CUDA_EonDevice_noalloc clear") != 0)
+    scratch_view(base, kNoAllocMaxCtas, s);
+    if (cgppd_check(cudaMemsetAsync(base, 0, 8, cudaStreamLegacy), "CUDA_EonDevice_noalloc clear") != 0 ||
+        cgppd_check(cudaMemsetAsync(s.gtickets, 0, 4 * scratch_groups(kNoAllocMaxCtas), cudaStreamLegacy),
+                    "CUDA_EonDevice_noalloc clear") != 0)
         return;
     if (launch_energy(false, residuePositions, residueMeta, datasetSize, table, &s, nullptr, 0, cudaStreamLegacy) != 0)
         return;

@@ -70,7 +70,7 @@ void unbindLJTexture(void);
  * device memory while they evaluate energies (code running inside another
  * framework's memory pool or under a fixed device-memory budget, or a loop that must
  * stay free of allocation calls): same arguments and result, but its scratch is a
- * static 136,688-byte device array owned by the library, so it calls no cudaMalloc or
+ * static 139,896-byte device array owned by the library, so it calls no cudaMalloc or
  * cudaFree.  datasetSize is limited to 16384 residues (larger sizes are rejected with
  * an error and *result = 0).  Every call looks up the array's device address on the
  * current device (a lookup allocates nothing, and stays right after cudaDeviceReset);

@@ -4,7 +4,7 @@ Hosts that run inside another framework's device-memory pool, under a fixed memo
 budget, or in a loop that must not allocate, call this variant instead of
 CUDA_EonDevice; it uses a static device array as scratch.  Its result must equal
 CUDA_EonDevice's on the same inputs, call after call, and both must be within 1e-5 of
-the FP64 oracle.  The largest accepted size (16384 residues: 128 tiles, 8511 CTAs)
+the FP64 oracle.  The largest accepted size (16384 residues: 128 tiles, 8384 CTAs)
 fills the static array exactly; one residue more is refused.  This file is collected
 last so that a failure here leaves every other test already run; it also passes alone.
 """
@@ -95,7 +95,7 @@ def test_noalloc_large_system(L, refdata):
 
 
 def test_noalloc_at_the_limit_and_above(L, refdata):
-    # 16384 residues: 128 tiles of 128, 8511 CTAs -- every CTA slot of the static array
+    # 16384 residues: 128 tiles of 128, 8384 CTAs -- every CTA slot of the static array
     pos, meta, box = lattice_packed(16384, 16384, 11)
     check_all(L, refdata, pos, meta, box)
     # one residue more is refused before anything is launched (no device memory is read)
