@@ -423,7 +423,8 @@ def dropin_leg(args, torch, flush, wl, peak_tflops):
     tflops = pairs * FLOP_PER_PAIR / (k_ms / 1000.0) / 1e12
     return {"entry": "CUDA_EonDevice(_async)", "kernel": "k_tile_energy", "workload": wl.name + ", replica 0",
             "residues": N, "padded": P, "pairs_per_call": pairs, "kernel_ms": k_ms,
-            "kernel_ms_note": "median over 20 bursts of 20 back-to-back async calls on one stream, per call",
+            "kernel_ms_note": "median over 20 bursts of 20 back-to-back async calls on one stream, per call "
+                              "(each a dependent launch that waits for the previous call to end)",
             "single_call_ms": float(np.median(singles)), "sync_call_ms": sync_ms,
             "pair_evals_per_s": pairs / (k_ms / 1000.0), "achieved_tflops": tflops, "frac": tflops / peak_tflops,
             "energy_kcal": res.value}

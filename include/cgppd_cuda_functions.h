@@ -50,7 +50,9 @@ void CUDA_EonDeviceNC(float4 *residuePositions, float4 *residueMeta, int *residu
  * the total in element 0 and zeros elsewhere, so the caller's host sum is unchanged.
  * Like the reference's asynchronous call it reports nothing back to the host: a residue
  * type outside 0..19 is read as type 0 without an error (the synchronous entry points
- * check the types and fail on such input). */
+ * check the types and fail on such input).  On a stream other than the legacy default
+ * one the launch is a programmatic dependent launch that waits for the stream's previous
+ * kernel before touching memory (plain stream ordering). */
 void CUDA_EonDevice_async(float4 *residuePositions, float4 *residueMeta, int *residueCount, int *moleculePositions,
                           int *moleculeCount, float *LJPotentials, float *device_result, int resultSize,
                           int blockSize, int datasetSize, int sharedMemSize, cudaStream_t stream);
