@@ -151,6 +151,39 @@ def test_random_systems_vs_oracle(L, refdata, case):
         assert abs(g - ref[2]) <= REL * abs(ref[2]) + ABS, (nc, g, ref)
 
 
+def test_async_calls_back_to_back_on_one_stream(L, refdata):
+    # consecutive asynchronous calls on one stream share its scratch and are dependent
+    # launches (each may be placed before the previous one ends): every call must still
+    # see only its own inputs and leave its own total
+    import torch
+    rng = np.random.default_rng(77)
+    box = 120.0
+    pos0, meta = synthetic_packed(rng, 6, [100, 250], box, 0.1, 5)
+    L.CUDA_setBoxDimension(box)
+    systems, outs, refs = [], [], []
+    for k in range(8):
+        pos = pos0.copy()
+        n = int((pos[:, 3] > -2.0).sum())
+        pos[:n, :3] += rng.normal(scale=0.3, size=(n, 3)).astype(np.float32)
+        refs.append(oracle.E_packed(oracle.FP64, pos, meta, refdata["lj_table"], box)[2])
+        systems.append((device_array(pos), device_array(meta)))
+    rs = pos0.shape[0] // 32
+    s = torch.cuda.Stream()
+    for k, (dp, dm) in enumerate(systems):
+        out = torch.full((rs * rs,), 7.0, dtype=torch.float32, device="cuda")
+        outs.append(out)
+        L.CUDA_EonDevice_async(ptr(dp), ptr(dm), None, None, None, None, ptr(out), rs, 32, pos0.shape[0], 0,
+                               ctypes.c_void_p(s.cuda_stream))
+    s.synchronize()
+    cgppd_gb300.check("EonDevice_async burst")
+    for k, out in enumerate(outs):
+        h = out.cpu().numpy()
+        assert np.all(h[1:] == 0.0)
+        # float32 output: its rounding on top of the 1e-5 bound
+        assert abs(float(h[0]) - refs[k]) <= REL * abs(refs[k]) + 1e-6 * abs(refs[k]) + ABS, (k, h[0], refs[k])
+    assert len(set(float(o[0].item()) for o in outs)) > 1  # the inputs differ, so do the totals
+
+
 def test_empty_and_unbound(L, refdata):
     # empty dataset -> 0 without a launch
     res = ctypes.c_double(5.0)
