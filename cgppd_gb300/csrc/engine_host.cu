@@ -748,6 +748,21 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     base.sample_log = nullptr;  // timing launches record no samples
     if (e->da)
         base.dastats = das.ptr;
+    // the clones back to the engine's state (on the engine's stream, before a timed launch)
+    auto restore = [&]() -> int {
+        auto back = [&](auto &dst, const auto &src) {
+            return cudaMemcpyAsync(dst.ptr, src.ptr, src.n * sizeof(*src.ptr), cudaMemcpyDeviceToDevice, e->own_stream);
+        };
+        cudaError_t err = cudaSuccess;
+        for (cudaError_t r : {back(pos, e->d_pos), back(rel, e->d_rel), back(cen, e->d_center), back(em, e->d_emat),
+                              back(in, e->d_intra), back(pot, e->d_potential), back(st, e->d_stats),
+                              back(sc, e->d_stepc), back(pc, e->d_pairc), back(ef, e->d_errflags)})
+            if (err == cudaSuccess)
+                err = r;
+        if (err == cudaSuccess && e->da)
+            err = back(das, e->d_dastats);
+        return cgppd_check(err, "autotune restore");
+    };
     const int clusters[8] = {1, 2, 3, 4, 5, 6, 8, 16}, thread_opts[3] = {128, 256, 512};
     const int steps = 16;
     cudaEvent_t ev0, ev1;
@@ -775,9 +790,13 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
                 continue;
             }
             // the marginal cost of a step: launches of n and 2n steps (n sized so that one
-            // takes about 1 ms after a short probe), each the faster of two, differenced so
-            // that the per-launch set-up (state load and write-back) drops out
+            // takes about 2 ms after a short probe), each the faster of two, differenced so
+            // that the per-launch set-up (state load and write-back) drops out.  Every timed
+            // launch starts from the same copy of the state, so every shape is timed on the
+            // same moves (a step's cost varies several-fold with the molecule it moves).
             auto time_launch = [&](int n_steps, float &ms_out) -> bool {
+                if (restore() != 0)
+                    return false;
                 cudaEventRecord(ev0, e->own_stream);
                 cudaError_t err = launch_mc_block(a, e->total_replicas, n_steps, T, e->smem, e->own_stream);
                 cudaEventRecord(ev1, e->own_stream);
@@ -792,7 +811,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
             if (!time_launch(steps, probe))
                 continue;
             const float probe_us = 1000.f * probe / steps;
-            const int n = std::max(steps, std::min(1024, (int)(1000.f / std::max(probe_us, 1e-3f))));
+            const int n = std::max(steps, std::min(2048, (int)(2000.f / std::max(probe_us, 1e-3f))));
             float t1 = 1e30f, t2 = 1e30f;
             bool ok = true;
             for (int rep = 0; rep < 2 && ok; ++rep) {

@@ -73,10 +73,27 @@ struct MoveDesc {
     uint32_t w_stage1;       // delayed acceptance: the surrogate stage's uniform draw
 };
 
+// The part of a move decision that depends on the draws alone (src/Molecule.cpp:146-504:
+// the molecule, the move type, the direction and its rotation, the flex residue and
+// branch, the local residue and the crankshaft flip), taken for 32 steps at a time by
+// the lanes of one warp; finish_move adds the part that reads the state.
+struct MovePre {
+    int m, ri, br_off, br_cnt;
+    int bits;       // type | kind << 4 | null move << 8 | crankshaft flip << 9
+    float R[9];     // the rotation (rotate, flex) or the unit direction in R[0..2]
+    uint32_t w_metro, w_stage1;
+};
+
+// Ring of draw-only decisions in shared memory: the entries of steps [32k, 32k + 32)
+// are filled during step 32k - 17 (the first 32 before the loop), half a ring ahead of
+// the step that reads them.
+constexpr int kRing = 64;
+
 struct SmemLayout {
     int table, mols, ipos, irel, iexcl, idisp, iq, ipq, iqq, ej, rowp, row;  // always
     int rcv;                                                         // clusters: pushed partial rows
     int rad;                                                         // bounding radius per molecule
+    int ring;                                                        // draw-only decisions (kRing)
     int lst[12];                                                     // resident + flexible: static lists
     int P, Q, ST, EX, CEN, EM, INTRA, ROWSUM, QP;                    // resident only
     int daW, daW1, daB, daW5, daH, daHS, daX, daP, daF, daSM;        // delayed acceptance only
@@ -141,6 +158,7 @@ __host__ __device__ inline SmemLayout smem_layout(int max_mol, int slice, int ma
     // [2 step parities][C source ranks][max_m + 1] (last entry: internal energy)
     L.rcv = off;    off = align16(off + (C > 1 ? 2 * C * (max_m + 1) * 8 : 0));
     L.rad = off;    off = align16(off + 4 * max_m);
+    L.ring = off;   off = align16(off + kRing * (int)sizeof(MovePre));
     L.P = L.Q = L.ST = L.EX = L.CEN = L.EM = L.INTRA = L.ROWSUM = L.QP = 0;
     if (resident) {
         L.P = off;      off += 16 * max_n;
@@ -602,17 +620,6 @@ __device__ __forceinline__ T ld_state(const T *p)
     return __ldcg(p);
 }
 
-// The part of a move decision that depends on the draws alone (src/Molecule.cpp:146-504:
-// the molecule, the move type, the direction and its rotation, the flex residue and
-// branch, the local residue and the crankshaft flip), taken one step ahead by a warp
-// that would otherwise wait; finish_move adds the part that reads the state.
-struct MovePre {
-    int m, type, kind, ri, br_off, br_cnt, null_move, flip;
-    float ux, uy, uz;
-    float R[9];
-    uint32_t w_metro, w_stage1;
-};
-
 __device__ void predecide_move(const Lists &a, const DevSim &S, const DevMol *mols, const float4 rsc,
                                const uint32_t *w, MovePre &pre)
 {
@@ -620,7 +627,8 @@ __device__ void predecide_move(const Lists &a, const DevSim &S, const DevMol *mo
     const int m = pickw(w[0], M);
     const DevMol &mol = mols[m];
     pre.m = m;
-    pre.kind = 0, pre.ri = 0, pre.br_off = 0, pre.br_cnt = 0, pre.null_move = 0, pre.flip = 0;
+    pre.ri = 0, pre.br_off = 0, pre.br_cnt = 0;
+    int kind = 0, null_move = 0, flip = 0;
     int type;
     if (mol.flags & kMolFlexible) {
         int k = 0;
@@ -636,13 +644,12 @@ __device__ void predecide_move(const Lists &a, const DevSim &S, const DevMol *mo
     } else {
         type = ((unsigned long long)w[1] < S.thr_rot) ? kRotate : kTranslate;  // gsl_ran_bernoulli
     }
-    pre.type = type;
     const float dx = centred(w[2], false), dy = centred(w[3], true), dz = centred(w[4], false);
     switch (type) {
     case kTranslate: {
         // Molecule::translate(rng, step) (src/Molecule.cpp:146-159, :262-266)
         const float3 u = normalized(dx, dy, dz);
-        pre.ux = u.x, pre.uy = u.y, pre.uz = u.z;
+        pre.R[0] = u.x, pre.R[1] = u.y, pre.R[2] = u.z;
         break;
     }
     case kRotate: {
@@ -654,14 +661,14 @@ __device__ void predecide_move(const Lists &a, const DevSim &S, const DevMol *mo
     case kFlex: {
         // Molecule::flex(rng, step) (src/Molecule.cpp:331-413)
         if (mol.nflex == 0) {
-            pre.null_move = 1;
+            null_move = 1;
             break;
         }
         const float3 u = normalized(dx, dy, dz);
         axis_angle_matrix_sc(rsc.x, rsc.y, u.x, u.y, u.z, false, pre.R);
         const int4 fr = a.flexres[mol.flex_off + pickw(w[5], mol.nflex) - a.base[kLFlex]];
         if (fr.y <= 0) {
-            pre.null_move = 1;
+            null_move = 1;
             break;
         }
         const int4 op = a.flexopt[fr.z + pickw(w[6], fr.y) - a.base[kLFopt]];
@@ -673,31 +680,32 @@ __device__ void predecide_move(const Lists &a, const DevSim &S, const DevMol *mo
     case kLocal: {
         // Molecule::make_local_moves (src/Molecule.cpp:415-448): Bernoulli(0.5) picks a
         // crankshaft (1) or a local translation (0) of one residue.
-        pre.kind = (w[5] < 2147483648u) ? 1 : 0;
-        if (pre.kind == 0) {
+        kind = (w[5] < 2147483648u) ? 1 : 0;
+        if (kind == 0) {
             if (mol.nlocal == 0) {
-                pre.null_move = 1;
+                null_move = 1;
                 break;
             }
             pre.ri = a.localres[mol.local_off + pickw(w[6], mol.nlocal) - a.base[kLLocal]];
             const float3 u = normalized(dx, dy, dz);
-            pre.ux = u.x, pre.uy = u.y, pre.uz = u.z;
+            pre.R[0] = u.x, pre.R[1] = u.y, pre.R[2] = u.z;
         } else {
             if (mol.ncrank == 0) {
-                pre.null_move = 1;
+                null_move = 1;
                 break;
             }
             const int ri = a.crankres[mol.crank_off + pickw(w[6], mol.ncrank) - a.base[kLCrank]];
             if (ri < 1 || ri + 1 >= mol.count) {  // needs both backbone neighbours in the array
-                pre.null_move = 1;
+                null_move = 1;
                 break;
             }
             pre.ri = ri;
-            pre.flip = w[7] < 2147483648u;
+            flip = w[7] < 2147483648u;
         }
         break;
     }
     }
+    pre.bits = type | (kind << 4) | (null_move << 8) | (flip << 9);
     pre.w_metro = w[8];
     pre.w_stage1 = w[9];
 }
@@ -710,17 +718,19 @@ __device__ void finish_move(const DevSim &S, const DevMol *mols, const float4 *C
 {
     const int m = pre.m;
     const DevMol &mol = mols[m];
+    const int ptype = pre.bits & 15, pkind = (pre.bits >> 4) & 15, pnull = (pre.bits >> 8) & 1,
+              pflip = (pre.bits >> 9) & 1;
     mv.m = m;
     mv.start = mol.start;
     mv.n = mol.count;
     mv.flexible = (mol.flags & kMolFlexible) != 0;
     mv.nintra = mol.nintra;
-    mv.type = pre.type;
-    mv.kind = pre.kind;
+    mv.type = ptype;
+    mv.kind = pkind;
     mv.ri = pre.ri;
     mv.br_off = pre.br_off;
     mv.br_cnt = pre.br_cnt;
-    mv.null_move = pre.null_move;
+    mv.null_move = pnull;
     mv.wrapped = 0;
     mv.w_metro = pre.w_metro;
     mv.w_stage1 = pre.w_stage1;
@@ -729,9 +739,9 @@ __device__ void finish_move(const DevSim &S, const DevMol *mols, const float4 *C
     mv.cx = c.x, mv.cy = c.y, mv.cz = c.z;
     mv.wcx = c.x, mv.wcy = c.y, mv.wcz = c.z;
     const float4 *Pm = P + mv.start;
-    switch (pre.type) {
+    switch (ptype) {
     case kTranslate:
-        mv.vx = pre.ux * tstep, mv.vy = pre.uy * tstep, mv.vz = pre.uz * tstep;
+        mv.vx = pre.R[0] * tstep, mv.vy = pre.R[1] * tstep, mv.vz = pre.R[2] * tstep;
         mv.wcx = wrapf(c.x + mv.vx, box);
         mv.wcy = wrapf(c.y + mv.vy, box);
         mv.wcz = wrapf(c.z + mv.vz, box);
@@ -742,7 +752,7 @@ __device__ void finish_move(const DevSim &S, const DevMol *mols, const float4 *C
             mv.R[k] = pre.R[k];
         break;
     case kFlex: {
-        if (pre.null_move)
+        if (pnull)
             break;
 #pragma unroll
         for (int k = 0; k < 9; ++k)
@@ -752,12 +762,12 @@ __device__ void finish_move(const DevSim &S, const DevMol *mols, const float4 *C
         break;
     }
     case kLocal: {
-        if (pre.null_move)
+        if (pnull)
             break;
         float vx, vy, vz;
-        if (pre.kind == 0) {
+        if (pkind == 0) {
             const float s = (float)((double)0.1f * (double)tstep);
-            vx = pre.ux * s, vy = pre.uy * s, vz = pre.uz * s;
+            vx = pre.R[0] * s, vy = pre.R[1] * s, vz = pre.R[2] * s;
         } else {
             const int ri = pre.ri;
             const float4 pm = ld_state<RES>(&Pm[ri - 1]);
@@ -765,7 +775,7 @@ __device__ void finish_move(const DevSim &S, const DevMol *mols, const float4 *C
             const float4 pp = ld_state<RES>(&Pm[ri + 1]);
             const float3 ax = normalized(pp.x - pm.x, pp.y - pm.y, pp.z - pm.z);
             float Rm[9];
-            axis_angle_matrix_sc(pre.flip ? rsc.z : rsc.x, pre.flip ? rsc.w : rsc.y, ax.x, ax.y, ax.z, true, Rm);
+            axis_angle_matrix_sc(pflip ? rsc.z : rsc.x, pflip ? rsc.w : rsc.y, ax.x, ax.y, ax.z, true, Rm);
             const float3 rr = rot_apply(Rm, p0.x - pm.x, p0.y - pm.y, p0.z - pm.z);
             vx = (rr.x + pm.x) - p0.x;
             vy = (rr.y + pm.y) - p0.y;
@@ -1021,7 +1031,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ MoveDesc mv;
-    __shared__ MovePre s_pre;      // the next step's draw-only decision
     __shared__ FF s_red[kMaxWarps];
     __shared__ float s_fred[3 * kMaxWarps];
     // running total, old/new row of the moved molecule and its internal energy, all as
@@ -1034,7 +1043,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     __shared__ int s_skip;         // ... 1 when stage 1 rejected it
     __shared__ DAStats s_da;
     __shared__ Lists s_lists;      // static-list views (shared: keeps them out of registers)
-    __shared__ uint32_t s_w[12];   // the next step's Philox words, drawn one step ahead
     __shared__ DaView s_dv;
 
     const int C = a.cluster;
@@ -1072,6 +1080,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     float2 *s_ej = reinterpret_cast<float2 *>(smem + Ly.ej);
     FF *s_rowp = reinterpret_cast<FF *>(smem + Ly.rowp);
     FF *s_row = reinterpret_cast<FF *>(smem + Ly.row);
+    MovePre *s_ring = reinterpret_cast<MovePre *>(smem + Ly.ring);
 
     const long long st0 = S.state_off + (long long)r * N;
     float4 *gP = a.pos + st0;
@@ -1157,17 +1166,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     float4 rsc;
     sincosf(0.5f * rstep, &rsc.x, &rsc.y);
     sincosf(-(0.5f * rstep), &rsc.z, &rsc.w);
-    // Philox words of step mcstep (counter (step, step_hi, lane, 'MC')), lanes 0-2 of a warp
-    auto draw = [&](unsigned long long mcstep) {
-        if (lane < 3) {
-            const U4 ctr{(uint32_t)mcstep, (uint32_t)(mcstep >> 32), (uint32_t)lane, 0x4D43u};
-            const U4 res = philox4x32_10(ctr, key0, key1);
-            s_w[4 * lane + 0] = res.x, s_w[4 * lane + 1] = res.y, s_w[4 * lane + 2] = res.z,
-                           s_w[4 * lane + 3] = res.w;
-        }
-    };
-    if (warp == 0)
-        draw(step0);
     // pair and error counters live in registers of thread 0 (rank 0 writes them back)
     unsigned long long pairs = 0;
     unsigned errbits = 0;
@@ -1262,35 +1260,32 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
         }
     }
 
-    // the first step's draw-only decision (later ones are taken a step ahead by the
-    // last warp while warp 0 runs the Metropolis test)
-    if (t == 0) {
+    // Draw-only decisions of the 32 steps from `first` (local step index), lane k taking
+    // step first + k: its Philox words (counter (step, step_hi, word block, 'MC')) and
+    // predecide_move, into the ring.  The last warp fills it: the first 32 steps here,
+    // the next ones during the Metropolis test of every 32nd step.
+    auto fill_ring = [&](int first) {
+        const int k = first + lane;
+        const unsigned long long ms = step0 + (unsigned long long)k;
         uint32_t w[12];
 #pragma unroll
-        for (int k = 0; k < 12; ++k)
-            w[k] = s_w[k];
-        predecide_move(Ls, S, s_mols, rsc, w, s_pre);
-    }
-    __syncthreads();
-    // the next step's words and draw-only decision, by the last warp
-    auto draw_ahead = [&](unsigned long long next) {
-        draw(next);
-        __syncwarp();
-        if (lane == 0) {
-            uint32_t w[12];
-#pragma unroll
-            for (int k = 0; k < 12; ++k)
-                w[k] = s_w[k];
-            predecide_move(Ls, S, s_mols, rsc, w, s_pre);
+        for (int b = 0; b < 3; ++b) {
+            const U4 ctr{(uint32_t)ms, (uint32_t)(ms >> 32), (uint32_t)b, 0x4D43u};
+            const U4 res = philox4x32_10(ctr, key0, key1);
+            w[4 * b + 0] = res.x, w[4 * b + 1] = res.y, w[4 * b + 2] = res.z, w[4 * b + 3] = res.w;
         }
+        predecide_move(Ls, S, s_mols, rsc, w, s_ring[k & (kRing - 1)]);
     };
+    if (warp == NW - 1)
+        fill_ring(0);
+    __syncthreads();
 
     for (int step = 0; step < nsteps; ++step) {
         const unsigned long long mcstep = step0 + (unsigned long long)step;
         // ---- the move decision (thread 0): the state-dependent part of the decision
         // taken a step ahead
         if (t == 0) {
-            finish_move<RES>(S, s_mols, CEN, P, tstep, rsc, s_pre, mv);
+            finish_move<RES>(S, s_mols, CEN, P, tstep, rsc, s_ring[step & (kRing - 1)], mv);
             if (RES)
                 s_old_row = ROWSUMf[mv.m];
         }
@@ -1773,8 +1768,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 if (nullm)
                     errbits |= 1u;
             }
-        } else if (warp == NW - 1) {
-            draw_ahead(mcstep + 1);  // (thread 0 consumed this step's decision before the first barrier)
+        } else if (warp == NW - 1 && (step & 31) == 15) {
+            fill_ring(step + 17);  // the steps of the next block of 32, half a ring ahead
         }
         __syncthreads();
 
@@ -1826,10 +1821,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
             }
         }
         }  // !skip
-        // a step the surrogate rejected skipped the Metropolis slot: the next step's words
-        // and decision here (the end-of-step barrier publishes them)
-        if (skip && warp == NW - 1)
-            draw_ahead(mcstep + 1);
+        // a step the surrogate rejected skipped the Metropolis slot: the ring's refill here
+        // (the end-of-step barrier publishes it)
+        if (skip && warp == NW - 1 && (step & 31) == 15)
+            fill_ring(step + 17);
         // fraction-bound sample (src/Simulation.cpp:1063-1073, src/Replica.cpp:1037-1063)
         const int freq = S.sample_freq;
         if (freq > 0 && (long long)(mcstep % (unsigned long long)freq) == freq - 1 &&
