@@ -135,7 +135,7 @@ def build_dropin_program(ref_root=None, lib_dir=None):
               "-I" + os.path.join(stubs, "cuda"), "-I" + stubs, "-I" + os.path.join(cuda, "include"), "-I" + src,
               "-o", DROPIN_OUT] + cpp +
              [obj, "-L" + lib_dir, "-lcgppd_gb300", "-L" + os.path.join(cuda, "lib64"), "-lcudart",
-              # setup_CUDA (src/Simulation.cpp) calls the driver's cuInit: the toolkit's link stub
+              # setup_CUDA (src/Simulation.cpp) calls cuInit of the CUDA driver API: the toolkit's link stub
               "-L" + os.path.join(cuda, "lib64", "stubs"), "-lcuda", "-lpthread",
               "-lm", "-Wl,-rpath," + lib_dir,
               "-Wl,--wrap=_ZN8Vector3fpLES_", "-Wl,--wrap=_ZN8Vector3fmIES_"]]
