@@ -41,7 +41,7 @@ namespace {
 // (64-residue tiles, four times the CTAs for a one-wave call, measured no faster:
 // 26.5-27.5 us against 24.7 us for a 6 M-pair call, with 12 % more instructions.)
 constexpr int kTile = 128;                 // residues per tile side
-constexpr int kThreads = 2 * kTile;        // two threads per y residue (x-tile halves)
+constexpr int kThreads = 2 * kTile;        // two threads per y residue (four for a half y tile)
 constexpr int kWarps = kThreads / 32;
 
 __constant__ float c_boxdim;  // CUDA_setBoxDimension, module state per device

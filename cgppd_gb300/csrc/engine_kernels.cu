@@ -1283,7 +1283,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
     for (int step = 0; step < nsteps; ++step) {
         const unsigned long long mcstep = step0 + (unsigned long long)step;
         // ---- the move decision (thread 0): the state-dependent part of the decision
-        // taken a step ahead
+        // whose draw-only part waits in the ring
         if (t == 0) {
             finish_move<RES>(S, s_mols, CEN, P, tstep, rsc, s_ring[step & (kRing - 1)], mv);
             if (RES)
