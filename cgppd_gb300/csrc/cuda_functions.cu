@@ -236,11 +236,11 @@ __device__ __forceinline__ void charged_first_pairs(const PairCtx &c, const floa
         lj_span<TESTED, S>(c, s_pq, s_qt, s_qk, j, e[3], lj);
 }
 
-// One warp's residues' exclusion-key ranges and flags, stored by lane 0 into wk[0..10]:
+// One warp's residues' exclusion-key ranges and flags, stored by lane 0 into wk[0..8]:
 // [nonzero domain min/max, nonzero bond min/max, chain min/max, molecule min/max] as
-// bit patterns, the OR of the flags (bit 0 padding, bit 1 crowder), and the domain
-// min/max over every real residue (zero included).  Ranges are of the keys' bit
-// patterns: two sets of floats whose bit-pattern ranges are disjoint share no value.
+// bit patterns, then the OR of the flags (bit 0 padding, bit 1 crowder).  Ranges are of
+// the keys' bit patterns: two sets of floats whose bit-pattern ranges are disjoint share
+// no value.
 __device__ __forceinline__ void warp_keys(int *wk, float dom, float bond, float chain, float mol, int flags)
 {
     const int inf = 0x7fffffff;
@@ -256,27 +256,23 @@ __device__ __forceinline__ void warp_keys(int *wk, float dom, float bond, float 
     for (int k = 0; k < 8; ++k)
         r[k] = (k & 1) ? __reduce_max_sync(0xffffffffu, v[k]) : __reduce_min_sync(0xffffffffu, v[k]);
     const int f = (int)__reduce_or_sync(0xffffffffu, (unsigned)flags);
-    const int dlo = __reduce_min_sync(0xffffffffu, real ? d : inf), dhi = __reduce_max_sync(0xffffffffu, real ? d : -1);
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
         for (int k = 0; k < 8; ++k)
             wk[k] = r[k];
         wk[8] = f;
-        wk[9] = dlo;
-        wk[10] = dhi;
     }
 }
 
-constexpr int kKeys = 11;
+constexpr int kKeys = 9;
 
-// Key k of a tile from the nw warps that stored theirs (OR for the flags, k = 8; else
-// min for the lower bounds 0, 2, 4, 6, 9 and max for the upper ones).
+// Key k of a tile from the nw warps that stored theirs (min for even k, max for odd k,
+// OR for the flags, k = 8).
 __device__ __forceinline__ int tile_key(const int (*wk)[kKeys], int nw, int k)
 {
-    const bool lower = (k < 8) ? (k & 1) == 0 : k == 9;
     int v = wk[0][k];
     for (int w = 1; w < nw; ++w)
-        v = (k == 8) ? (v | wk[w][k]) : lower ? min(v, wk[w][k]) : max(v, wk[w][k]);
+        v = (k == 8) ? (v | wk[w][k]) : (k & 1) ? max(v, wk[w][k]) : min(v, wk[w][k]);
     return v;
 }
 
