@@ -324,12 +324,12 @@ __global__ void __launch_bounds__(kThreads) k_tile_energy(const float4 *__restri
     __shared__ float s_m4[400];   // -4 Eij in RT units (the clean-tile loop's form)
     __shared__ FF s_red[2][kWarps];
     __shared__ bool s_last, s_last_group;
-    // the x tile again in charged-first order (position + radius, charge + type) for
-    // tile pairs without any excluded pair
+    // the x tile's real residues again in charged-first order (position + half radius,
+    // charge + type), for the charged-first loop
     __shared__ float4 s_pq[kTile];
     __shared__ float2 s_qt[kTile];
-    // ... and its exclusion keys (domain, bond, chain, original index | padding << 16) for
-    // tile pairs that may hold excluded pairs (default potential)
+    // ... and their exclusion keys (domain, bond, chain, original index), for the pairs
+    // that take the exclusion tests
     __shared__ float4 s_qk[kTile];
     // per-warp key ranges and flags of the x tile and of this CTA's y residues (warp_keys)
     __shared__ int s_wk[2][kTile / 32][kKeys];
