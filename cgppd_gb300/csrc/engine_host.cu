@@ -172,6 +172,8 @@ struct cgppd_engine {
     DevBuf<SampleRec> d_sample_log;  // boundconformations records (cgppd_engine_set_sample_log)
     DevBuf<unsigned> d_sample_count;
     int sample_cap = 0;
+    DevBuf<float4> d_sample_xyz;     // their coordinates (cgppd_engine_set_sample_snapshots)
+    int sample_nres = 0;
 
     std::vector<DevSim> h_sims;
     std::vector<DevMol> h_mols;
@@ -236,6 +238,8 @@ struct cgppd_engine {
         a.sample_log = sample_cap > 0 ? d_sample_log.ptr : nullptr;
         a.sample_count = d_sample_count.ptr;
         a.sample_cap = sample_cap;
+        a.sample_xyz = (sample_cap > 0 && sample_nres > 0) ? d_sample_xyz.ptr : nullptr;
+        a.sample_nres = sample_nres;
         a.seed_lo = (uint32_t)seed;
         a.seed_hi = (uint32_t)(seed >> 32);
         a.ntypes = ntypes;
@@ -746,6 +750,7 @@ static int autotune(cgppd_engine *e, int fixed_cluster, int fixed_threads)
     base.pos = pos.ptr, base.rel = rel.ptr, base.center = cen.ptr, base.emat = em.ptr, base.intra = in.ptr;
     base.potential = pot.ptr, base.stats = st.ptr, base.stepc = sc.ptr, base.pairc = pc.ptr, base.errflags = ef.ptr;
     base.sample_log = nullptr;  // timing launches record no samples
+    base.sample_xyz = nullptr;
     if (e->da)
         base.dastats = das.ptr;
     // the clones back to the engine's state (on the engine's stream, before a timed launch)
@@ -1452,15 +1457,59 @@ int cgppd_engine_set_sample_log(cgppd_engine *e, int per_replica)
         return -1;
     e->sample_cap = 0;
     e->d_sample_log.release();
+    e->d_sample_xyz.release();
     if (per_replica > 0) {
         if (e->d_sample_log.alloc((size_t)per_replica * e->total_replicas) != 0 ||
-            e->d_sample_count.zero((size_t)e->total_replicas) != 0)
+            e->d_sample_count.zero((size_t)e->total_replicas) != 0 ||
+            (e->sample_nres > 0 &&
+             e->d_sample_xyz.alloc((size_t)per_replica * e->total_replicas * e->sample_nres) != 0))
             return -1;
         e->sample_cap = per_replica;
     }
     for (auto &kv : e->graphs)  // graphs captured the old arguments
         cudaGraphExecDestroy(kv.second);
     e->graphs.clear();
+    return 0;
+}
+
+int cgppd_engine_set_sample_snapshots(cgppd_engine *e, int residues)
+{
+    if (!e || !e->finalized || residues < 0)
+        return cgppd_fail("cgppd_engine_set_sample_snapshots: engine not finalized or negative residue count");
+    if (cgppd_check(cudaDeviceSynchronize(), "sample snapshots") != 0)
+        return -1;
+    e->d_sample_xyz.release();
+    e->sample_nres = 0;
+    if (residues > 0 && e->sample_cap > 0 &&
+        e->d_sample_xyz.alloc((size_t)e->sample_cap * e->total_replicas * residues) != 0)
+        return -1;
+    e->sample_nres = residues;
+    for (auto &kv : e->graphs)  // graphs captured the old arguments
+        cudaGraphExecDestroy(kv.second);
+    e->graphs.clear();
+    return 0;
+}
+
+int cgppd_engine_take_sample_xyz(cgppd_engine *e, int sim, float *xyz)
+{
+    if (!e || sim < 0 || sim >= (int)e->h_sims.size() || !xyz)
+        return cgppd_fail("cgppd_engine_take_sample_xyz: bad simulation index or output");
+    if (e->sample_cap <= 0 || e->sample_nres <= 0)
+        return 0;
+    if (cgppd_check(cudaDeviceSynchronize(), "take sample coordinates") != 0)
+        return -1;
+    const DevSim &S = e->h_sims[sim];
+    const size_t n = (size_t)S.R * e->sample_cap * e->sample_nres;
+    std::vector<float4> h(n);
+    if (cgppd_check(cudaMemcpy(h.data(), e->d_sample_xyz.ptr + (size_t)S.rep_off * e->sample_cap * e->sample_nres,
+                               sizeof(float4) * n, cudaMemcpyDeviceToHost),
+                    "take sample coordinates") != 0)
+        return -1;
+    for (size_t i = 0; i < n; ++i) {
+        xyz[3 * i] = h[i].x;
+        xyz[3 * i + 1] = h[i].y;
+        xyz[3 * i + 2] = h[i].z;
+    }
     return 0;
 }
 

@@ -1843,6 +1843,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                 } else if (S.nc_mode == 2) {
                     e = ff_value(s_pot);
                 }
+                int slot = -1;  // this sample's record in the log
                 if (lane == 0) {
                     st.samplesSinceLastExchange++;
                     if ((float)e < S.bound_threshold)
@@ -1854,9 +1855,21 @@ __global__ void __launch_bounds__(kMaxThreads) k_mc(EngineArgs a, int nsteps)
                             a.sample_log[(long long)g * a.sample_cap + k] =
                                 SampleRec{e, ff_value(s_pot), temperature, (int)(mcstep + 1 - (unsigned)freq)};
                             a.sample_count[g] = k + 1;
+                            slot = (int)k;
                         } else {
                             errbits |= 8u;  // log full: the sample is counted but not recorded
                         }
+                    }
+                }
+                // and its coordinates (the sample PDB of src/Replica.cpp:1082-1087, 1124-1168),
+                // when the host keeps them: the leading residues, the non-crowders
+                slot = __shfl_sync(0xffffffffu, slot, 0);
+                if (slot >= 0 && a.sample_xyz != nullptr) {
+                    const int nres = min(a.sample_nres, N);
+                    float4 *dst = a.sample_xyz + ((long long)g * a.sample_cap + slot) * a.sample_nres;
+                    for (int i = lane; i < nres; i += 32) {
+                        const float4 p = ld_state<RES>(&P[i]);
+                        dst[i] = make_float4(p.x, p.y, p.z, 0.f);
                     }
                 }
             }

@@ -145,6 +145,8 @@ struct EngineArgs {
     SampleRec *sample_log;       // [total replicas][sample_cap] or null
     unsigned *sample_count;      // records held per replica
     int sample_cap;
+    float4 *sample_xyz;          // [total replicas][sample_cap][sample_nres] coordinates, or null
+    int sample_nres;             // leading residues of a replica kept per record
     uint32_t seed_lo, seed_hi;
     int ntypes;
     int cluster;                 // CTAs per replica

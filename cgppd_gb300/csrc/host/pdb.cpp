@@ -4,6 +4,7 @@
 #include "../status.h"
 #include "cgppd_pdb.h"
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -121,24 +122,32 @@ PlacedMolecule place_molecule(const std::vector<PdbResidue> &res, int num_chains
 }
 
 void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float *pos, const AminoAcids &aa,
-                     int *atom_counter)
+                     int *atom_counter, int chain_base)
 {
+    // the three-letter name in capitals, as AminoAcid::getSNAME gives it (src/AminoAcid.cpp:19-25)
+    auto sname = [&](int type, char *buf) {
+        for (int k = 0; k < 3; ++k)
+            buf[k] = (char)std::toupper((unsigned char)aa.data[type].sname[k]);
+        buf[3] = 0;
+        return buf;
+    };
+    char b0[4], b1[4];
     char last_chain = 0;
     int last_seq = 0;
     for (size_t i = 0; i < res.size(); ++i) {
-        const char chain = (char)(65 + res[i].chain_index);
+        const char chain = (char)(65 + chain_base + res[i].chain_index);
         if (i > 0 && chain != last_chain)
-            std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, aa.data[res[i - 1].type].sname, last_chain,
+            std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, sname(res[i - 1].type, b0), last_chain,
                          last_seq);
         ++*atom_counter;
         std::fprintf(out, "ATOM  %5d CA   %3s %c%4d    %8.3f%8.3f%8.3f%6.2f%6.2f\n", *atom_counter,
-                     aa.data[res[i].type].sname, chain, res[i].res_seq, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2],
-                     0.0f, 0.0f);
+                     sname(res[i].type, b1), chain, res[i].res_seq, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f,
+                     0.0f);
         last_seq = res[i].res_seq;
         last_chain = chain;
     }
     if (!res.empty())
-        std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, aa.data[res.back().type].sname, last_chain,
+        std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, sname(res.back().type, b0), last_chain,
                      last_seq);
 }
 

@@ -38,7 +38,10 @@ PlacedMolecule place_molecule(const std::vector<PdbResidue> &res, int num_chains
                               float pz, float rx, float ry, float rz, float angle, float box);
 
 // Reference PDB output of one molecule's C-alpha trace (src/Replica.cpp:1124-1168 format).
+// Chain letters are replica-wide, as the reference's chain UIDs (src/Geometry.cpp:256-297):
+// 'A' + chain_base + the residue's chain index, chain_base counting the chains of the
+// molecules before this one.
 void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float *pos, const AminoAcids &aa,
-                     int *atom_counter);
+                     int *atom_counter, int chain_base = 0);
 
 }  // namespace cgppd

@@ -497,6 +497,12 @@ void Simulation::write_samples(int steps_per_block, int cap)
             order.emplace_back(step[o] / steps_per_block, r, step[o], o);
         }
     std::sort(order.begin(), order.end());
+    // every sample's conformation (the reference's build records all samples,
+    // src/definitions.h:36): the non-crowder molecules, which lead the replica
+    const int nres = sample_residues();
+    std::vector<float> xyz((size_t)R * cap * nres * 3);
+    if (nres > 0 && cgppd_engine_take_sample_xyz(engine_, 0, xyz.data()) != 0)
+        throw "MC run failed.";
     char name[512];
     for (const auto &x : order) {
         const size_t o = std::get<3>(x);
@@ -504,8 +510,42 @@ void Simulation::write_samples(int steps_per_block, int cap)
                       (double)temp[o], enc[o]);
         std::fprintf(boundConformationsFile, "%d; %0.5f (%0.5f); %0.1f\n%s\n", step[o], enc[o], pot[o],
                      (double)temp[o], name);
+        if (nres > 0)
+            write_sample_pdb(name, temp[o], step[o], pot[o], xyz.data() + o * nres * 3);
     }
     std::fflush(boundConformationsFile);
+}
+
+// Residues of the molecules before the first crowder (the part of a replica a sample
+// PDB holds).
+int Simulation::sample_residues() const
+{
+    int n = 0;
+    for (size_t k = 0; k < molecules.size() && !parameters.mdata[k].crowder; ++k)
+        n += (int)molecules[k].residues.size();
+    return n;
+}
+
+// Replica::saveAsSinglePDB (src/Replica.cpp:1124-1168): the sample's header, then the
+// C-alpha trace of the molecules before the first crowder at the sampled coordinates.
+void Simulation::write_sample_pdb(const char *path, float temperature_k, int step, double potential,
+                                  const float *xyz) const
+{
+    FILE *f = std::fopen(path, "w");
+    if (!f)
+        return;
+    std::fprintf(f, "REMARK simulation: %s \n", parameters.prefix.c_str());
+    std::fprintf(f, "REMARK temperature: %5.1f \n", (double)temperature_k);
+    std::fprintf(f, "REMARK sample: %d \n", step);
+    std::fprintf(f, "REMARK potential: %0.10f \n", (double)(float)potential);
+    int counter = 0, chain_base = 0, off = 0;
+    for (size_t k = 0; k < molecules.size() && !parameters.mdata[k].crowder; ++k) {
+        write_pdb_atoms(f, molecules[k].residues, xyz + 3 * off, aminoAcidData, &counter, chain_base);
+        chain_base += molecules[k].num_chains;
+        off += (int)molecules[k].residues.size();
+    }
+    std::fprintf(f, "END \n");
+    std::fclose(f);
 }
 
 // Simulation::run (src/Simulation.cpp:709-873): REsteps blocks of MCsteps/REsteps MC
@@ -526,7 +566,8 @@ void Simulation::run()
     int chunk = RE;
     if (per_block > 0) {
         chunk = std::max(1, std::min(RE, 4096 / per_block));
-        if (cgppd_engine_set_sample_log(engine_, chunk * per_block) != 0)
+        if (cgppd_engine_set_sample_snapshots(engine_, sample_residues()) != 0 ||
+            cgppd_engine_set_sample_log(engine_, chunk * per_block) != 0)
             throw "MC run failed.";
     }
     for (int b = 0; b < RE; b += chunk) {
@@ -560,10 +601,11 @@ void Simulation::run()
     if (f) {
         std::fprintf(f, "REMARK simulation: %s \n", parameters.prefix.c_str());
         std::fprintf(f, "REMARK temperature: %5.1f \n", temperature[0]);
-        int counter = 0, off = 0;
+        int counter = 0, off = 0, chain_base = 0;
         for (size_t k = 0; k < molecules.size(); ++k) {
             if (!parameters.mdata[k].crowder)
-                write_pdb_atoms(f, molecules[k].residues, xyz.data() + 3 * off, aminoAcidData, &counter);
+                write_pdb_atoms(f, molecules[k].residues, xyz.data() + 3 * off, aminoAcidData, &counter, chain_base);
+            chain_base += molecules[k].num_chains;
             off += (int)molecules[k].residues.size();
         }
         std::fprintf(f, "END \n");

@@ -51,6 +51,8 @@ _DECL = {
     "cgppd_engine_set_sample_log": (c_int, [c_void_p, c_int]),
     "cgppd_engine_take_samples": (c_int, [c_void_p, c_int, P(c_int), P(ctypes.c_double), P(ctypes.c_double),
                                           P(c_float), P(c_int)]),
+    "cgppd_engine_set_sample_snapshots": (c_int, [c_void_p, c_int]),
+    "cgppd_engine_take_sample_xyz": (c_int, [c_void_p, c_int, P(c_float)]),
 }
 
 
@@ -263,12 +265,25 @@ class Engine:
         _ok(_L().cgppd_engine_take_samples(self.h, sim, _p(counts, c_int), _p(enc, ctypes.c_double),
                                            _p(pot, ctypes.c_double), _p(temp, c_float), _p(step, c_int)),
             "take_samples")
+        xyz = None
+        if getattr(self, "_sample_nres", 0) > 0 and getattr(self, "_sample_cap", 0) > 0:
+            xyz = np.zeros((R, cap, self._sample_nres, 3), np.float32)
+            _ok(_L().cgppd_engine_take_sample_xyz(self.h, sim, _p(xyz, c_float)), "take_sample_xyz")
         out = []
         for r in range(R):
             sl = slice(r * cap, r * cap + counts[r])
-            out.append({"step": step[sl].copy(), "enc": enc[sl].copy(), "potential": pot[sl].copy(),
-                        "temperature": temp[sl].copy()})
+            rec = {"step": step[sl].copy(), "enc": enc[sl].copy(), "potential": pot[sl].copy(),
+                   "temperature": temp[sl].copy()}
+            if xyz is not None:
+                rec["xyz"] = xyz[r, :counts[r]].copy()
+            out.append(rec)
         return out
+
+    def set_sample_snapshots(self, residues):
+        """Keep the coordinates of the first `residues` residues with every recorded sample
+        (returned by take_samples as "xyz")."""
+        self._sample_nres = int(residues)
+        _ok(_L().cgppd_engine_set_sample_snapshots(self.h, int(residues)), "set_sample_snapshots")
 
     def checkpoint(self, path):
         _ok(_L().cgppd_engine_checkpoint(self.h, str(path).encode()), "checkpoint")

@@ -162,6 +162,16 @@ int cgppd_engine_set_sample_log(cgppd_engine *e, int per_replica);
 int cgppd_engine_take_samples(cgppd_engine *e, int sim, int *counts, double *enc, double *potential,
                               float *temperature, int *step);
 
+/* Coordinates of the samples, for the reference's sample PDB files
+ * (src/Replica.cpp:1082-1087, 1124-1168): after set_sample_snapshots(residues) every
+ * recorded sample also keeps the coordinates of the first `residues` residues of its
+ * replica (the non-crowders; 0 = none, the default).  take_sample_xyz copies one
+ * simulation's: xyz [n_replicas][per_replica][residues][3], slot r's record k at
+ * [r][k] -- the records that take_samples returned last (call it after take_samples and
+ * before the next run). */
+int cgppd_engine_set_sample_snapshots(cgppd_engine *e, int residues);
+int cgppd_engine_take_sample_xyz(cgppd_engine *e, int sim, float *xyz);
+
 /* MC steps done and residue-pair terms evaluated by all replicas since creation. */
 int cgppd_engine_counters(cgppd_engine *e, unsigned long long *mc_steps, unsigned long long *pair_evals);
 

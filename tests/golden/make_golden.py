@@ -242,7 +242,23 @@ def remc_outputs(ref, arch):
             per_t.setdefault(f[2].strip(), []).append(e)
         out["sampled_energy_mean_by_temperature"] = {t: sum(v) / len(v) for t, v in per_t.items()}
         out["sampled_energy_count_by_temperature"] = {t: len(v) for t, v in per_t.items()}
+        # the sample PDB files (src/Replica.cpp:1082-1087, 1124-1168): how many, and the
+        # layout of the first sample's file with its coordinates and values masked
+        out["pdb_sample_count"] = sum(1 for n in tf.getnames()
+                                      if n.startswith("remctest_%s/pdb/sample_" % arch))
+        out["pdb_sample_layout"] = [mask_pdb_line(ln) for ln in
+                                    text("pdb/" + os.path.basename(bc[3])).splitlines()]
     return out
+
+
+def mask_pdb_line(ln):
+    """A sample PDB line without what differs between runs: the coordinates of ATOM
+    records and the values of the REMARK records."""
+    if ln.startswith("ATOM"):
+        return ln[:30] + "*" + ln[54:]
+    if ln.startswith("REMARK") and ":" in ln and not ln.startswith("REMARK simulation"):
+        return ln.split(":")[0] + ":*"
+    return ln
 
 
 def main():

@@ -433,3 +433,25 @@ def test_sample_log_records_every_sample():
     assert all(len(x["step"]) == 25 for x in e.take_samples(0))
     assert e.error_bits() & 8
     e.close()
+
+
+@pytest.mark.parametrize("resident", [True, False])
+def test_sample_snapshots_hold_the_sampled_coordinates(resident):
+    # with snapshots on, every recorded sample also keeps the leading residues'
+    # coordinates (the sample PDB files): a sample on a block's last step holds the
+    # coordinates the replica ends the block with; C1's flexible molecule in a cluster
+    wl = workloads.make("c1")
+    sim = subset(wl, 3)
+    e = engine_for(wl, [sim], cluster=2, sample_frequency=50, sample_after=0, resident=resident)
+    nres = 100  # a prefix of the molecule: the first residues of the replica
+    e.set_sample_log(8)
+    e.set_sample_snapshots(nres)
+    for b in range(3):
+        e.run(1, 50, exchange_after_last=False)
+        rec = e.take_samples(0)
+        for r in range(3):
+            assert list(rec[r]["step"]) == [50 * b]
+            xyz, _, _ = e.state(0, r)
+            assert np.array_equal(rec[r]["xyz"][0], xyz[:nres])
+    assert e.error_bits() == 0
+    e.close()

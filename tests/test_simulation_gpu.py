@@ -12,6 +12,7 @@ potential of the samples at each temperature (boundconformations).
 """
 import ctypes
 import os
+import re
 
 import numpy as np
 import pytest
@@ -93,6 +94,30 @@ def test_output_files_match_reference_layout(workdir, refdata):
     labels = [int(ln.split(":")[0]) for ln in acc_lines[2:] if ":" in ln]
     assert labels == list(range(10, 1001, 10))
     assert (out / "pdb" / "final_lowest_temperature.pdb").exists()
+    # every sample line names its PDB file (the reference records all samples), laid out
+    # as the reference's: header, the non-crowders' C-alpha records in replica-wide
+    # chains, TER records, END (coordinates and header values masked)
+    names = [ln for ln in bc[3::2]]
+    assert len(names) == gold["pdb_sample_count"]
+    for name in names:
+        assert (workdir / name).exists(), name
+    first = open(workdir / names[0]).read().splitlines()
+    assert [mask_pdb_line(ln) for ln in first] == gold["pdb_sample_layout"]
+    # its potential header is the sample line's replica potential (a float printed with
+    # 10 decimals; the sample line prints 5)
+    pot = float(bc[2].split("(")[1].split(")")[0])
+    assert re.fullmatch(r"REMARK potential: -?\d+\.\d{10} ", first[3]), first[3]
+    assert abs(float(first[3].split(":")[1]) - pot) <= 5e-6 + 1e-6 * abs(pot)
+
+
+def mask_pdb_line(ln):
+    """tests/golden/make_golden.py: a sample PDB line without the coordinates of ATOM
+    records and the values of the REMARK records."""
+    if ln.startswith("ATOM"):
+        return ln[:30] + "*" + ln[54:]
+    if ln.startswith("REMARK") and ":" in ln and not ln.startswith("REMARK simulation"):
+        return ln.split(":")[0] + ":*"
+    return ln
 
 
 def test_statistics_within_spread_of_reference(workdir, refdata):
