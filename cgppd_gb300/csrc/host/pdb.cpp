@@ -121,8 +121,8 @@ PlacedMolecule place_molecule(const std::vector<PdbResidue> &res, int num_chains
     return m;
 }
 
-void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float *pos, const AminoAcids &aa,
-                     int *atom_counter, int chain_base)
+void write_pdb_trace(FILE *out, int n, const float *xyz, const int *types, const int *res_seq, const int *chain,
+                     const int *molecule, const AminoAcids &aa, int *atom_counter)
 {
     // the three-letter name in capitals, as AminoAcid::getSNAME gives it (src/AminoAcid.cpp:19-25)
     auto sname = [&](int type, char *buf) {
@@ -131,24 +131,44 @@ void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float 
         buf[3] = 0;
         return buf;
     };
-    char b0[4], b1[4];
-    char last_chain = 0;
-    int last_seq = 0;
-    for (size_t i = 0; i < res.size(); ++i) {
-        const char chain = (char)(65 + chain_base + res[i].chain_index);
-        if (i > 0 && chain != last_chain)
-            std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, sname(res[i - 1].type, b0), last_chain,
-                         last_seq);
+    char nm[4];
+    for (int i = 0; i < n; ++i) {
+        const char c = (char)(65 + chain[i]);
+        if (i > 0 && molecule[i] == molecule[i - 1] && chain[i] != chain[i - 1])
+            std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, sname(types[i - 1], nm),
+                         (char)(65 + chain[i - 1]), res_seq[i - 1]);
         ++*atom_counter;
         std::fprintf(out, "ATOM  %5d CA   %3s %c%4d    %8.3f%8.3f%8.3f%6.2f%6.2f\n", *atom_counter,
-                     sname(res[i].type, b1), chain, res[i].res_seq, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f,
-                     0.0f);
-        last_seq = res[i].res_seq;
-        last_chain = chain;
+                     sname(types[i], nm), c, res_seq[i], xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f, 0.0f);
+        if (i + 1 == n || molecule[i + 1] != molecule[i])
+            std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, sname(types[i], nm), c, res_seq[i]);
     }
-    if (!res.empty())
-        std::fprintf(out, "TER   %5d      %3s %c%4d \n", *atom_counter, sname(res.back().type, b0), last_chain,
-                     last_seq);
+}
+
+void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float *pos, const AminoAcids &aa,
+                     int *atom_counter, int chain_base)
+{
+    const int n = (int)res.size();
+    std::vector<int> types(n), seq(n), chain(n), molecule(n, 0);
+    for (int i = 0; i < n; ++i) {
+        types[i] = res[i].type;
+        seq[i] = res[i].res_seq;
+        chain[i] = chain_base + res[i].chain_index;
+    }
+    write_pdb_trace(out, n, pos, types.data(), seq.data(), chain.data(), molecule.data(), aa, atom_counter);
+}
+
+void write_sample_pdb(FILE *out, const char *title, float temperature, int sample, double potential, int n,
+                      const float *xyz, const int *types, const int *res_seq, const int *chain, const int *molecule,
+                      const AminoAcids &aa)
+{
+    std::fprintf(out, "REMARK simulation: %s \n", title);
+    std::fprintf(out, "REMARK temperature: %5.1f \n", (double)temperature);
+    std::fprintf(out, "REMARK sample: %d \n", sample);
+    std::fprintf(out, "REMARK potential: %0.10f \n", (double)(float)potential);
+    int counter = 0;
+    write_pdb_trace(out, n, xyz, types, res_seq, chain, molecule, aa, &counter);
+    std::fprintf(out, "END \n");
 }
 
 }  // namespace cgppd
@@ -186,4 +206,21 @@ extern "C" int cgppd_pdb_read(const char *path, const AminoAcids *a, int capacit
     if (num_chains)
         *num_chains = chains;
     return n;
+}
+
+extern "C" int cgppd_pdb_write_sample(const char *path, const AminoAcids *a, const char *title, float temperature,
+                                      int sample, double potential, int n, const float *xyz, const int *types,
+                                      const int *res_seq, const int *chain, const int *molecule)
+{
+    if (!path || !a || !title || n < 0 || (n > 0 && (!xyz || !types || !res_seq || !chain || !molecule)))
+        return cgppd_fail("cgppd_pdb_write_sample: path, table, title and n residue records are required");
+    for (int i = 0; i < n; ++i)
+        if (types[i] < 0 || types[i] >= 20 || chain[i] < 0 || chain[i] > 25)
+            return cgppd_fail("cgppd_pdb_write_sample: residue type outside 0..19 or chain outside A..Z");
+    FILE *f = std::fopen(path, "w");
+    if (!f)
+        return cgppd_fail("cgppd_pdb_write_sample: cannot open the output file");
+    cgppd::write_sample_pdb(f, title, temperature, sample, potential, n, xyz, types, res_seq, chain, molecule, *a);
+    std::fclose(f);
+    return 0;
 }

@@ -44,4 +44,17 @@ PlacedMolecule place_molecule(const std::vector<PdbResidue> &res, int num_chains
 void write_pdb_atoms(FILE *out, const std::vector<PdbResidue> &res, const float *pos, const AminoAcids &aa,
                      int *atom_counter, int chain_base = 0);
 
+// The same records for n residues given as arrays: types, residue numbers, replica-wide
+// chain numbers (0 = 'A') and molecule numbers (a TER record follows each molecule and
+// every chain change inside one).
+void write_pdb_trace(FILE *out, int n, const float *xyz, const int *types, const int *res_seq, const int *chain,
+                     const int *molecule, const AminoAcids &aa, int *atom_counter);
+
+// Replica::saveAsSinglePDB (src/Replica.cpp:1124-1168): the sample's header (simulation
+// title, temperature, sample step, the replica potential as a float), its C-alpha
+// records (write_pdb_trace), END.
+void write_sample_pdb(FILE *out, const char *title, float temperature, int sample, double potential, int n,
+                      const float *xyz, const int *types, const int *res_seq, const int *chain, const int *molecule,
+                      const AminoAcids &aa);
+
 }  // namespace cgppd

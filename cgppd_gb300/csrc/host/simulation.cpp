@@ -503,6 +503,18 @@ void Simulation::write_samples(int steps_per_block, int cap)
     std::vector<float> xyz((size_t)R * cap * nres * 3);
     if (nres > 0 && cgppd_engine_take_sample_xyz(engine_, 0, xyz.data()) != 0)
         throw "MC run failed.";
+    // the residues' records: types, numbers, replica-wide chains (src/Geometry.cpp:256-297),
+    // molecules
+    std::vector<int> types, seq, chain, mol;
+    for (size_t k = 0, chain_base = 0; k < molecules.size() && !parameters.mdata[k].crowder; ++k) {
+        for (const auto &r : molecules[k].residues) {
+            types.push_back(r.type);
+            seq.push_back(r.res_seq);
+            chain.push_back((int)chain_base + r.chain_index);
+            mol.push_back((int)k);
+        }
+        chain_base += molecules[k].num_chains;
+    }
     char name[512];
     for (const auto &x : order) {
         const size_t o = std::get<3>(x);
@@ -510,8 +522,14 @@ void Simulation::write_samples(int steps_per_block, int cap)
                       (double)temp[o], enc[o]);
         std::fprintf(boundConformationsFile, "%d; %0.5f (%0.5f); %0.1f\n%s\n", step[o], enc[o], pot[o],
                      (double)temp[o], name);
-        if (nres > 0)
-            write_sample_pdb(name, temp[o], step[o], pot[o], xyz.data() + o * nres * 3);
+        if (nres > 0) {
+            FILE *f = std::fopen(name, "w");
+            if (f) {
+                write_sample_pdb(f, parameters.prefix.c_str(), temp[o], step[o], pot[o], nres, xyz.data() + o * nres * 3,
+                                 types.data(), seq.data(), chain.data(), mol.data(), aminoAcidData);
+                std::fclose(f);
+            }
+        }
     }
     std::fflush(boundConformationsFile);
 }
@@ -524,28 +542,6 @@ int Simulation::sample_residues() const
     for (size_t k = 0; k < molecules.size() && !parameters.mdata[k].crowder; ++k)
         n += (int)molecules[k].residues.size();
     return n;
-}
-
-// Replica::saveAsSinglePDB (src/Replica.cpp:1124-1168): the sample's header, then the
-// C-alpha trace of the molecules before the first crowder at the sampled coordinates.
-void Simulation::write_sample_pdb(const char *path, float temperature_k, int step, double potential,
-                                  const float *xyz) const
-{
-    FILE *f = std::fopen(path, "w");
-    if (!f)
-        return;
-    std::fprintf(f, "REMARK simulation: %s \n", parameters.prefix.c_str());
-    std::fprintf(f, "REMARK temperature: %5.1f \n", (double)temperature_k);
-    std::fprintf(f, "REMARK sample: %d \n", step);
-    std::fprintf(f, "REMARK potential: %0.10f \n", (double)(float)potential);
-    int counter = 0, chain_base = 0, off = 0;
-    for (size_t k = 0; k < molecules.size() && !parameters.mdata[k].crowder; ++k) {
-        write_pdb_atoms(f, molecules[k].residues, xyz + 3 * off, aminoAcidData, &counter, chain_base);
-        chain_base += molecules[k].num_chains;
-        off += (int)molecules[k].residues.size();
-    }
-    std::fprintf(f, "END \n");
-    std::fclose(f);
 }
 
 // Simulation::run (src/Simulation.cpp:709-873): REsteps blocks of MCsteps/REsteps MC

@@ -92,7 +92,6 @@ private:
     void exchange_frequency(int steps, int row);
     void write_samples(int steps_per_block, int log_capacity);
     int sample_residues() const;
-    void write_sample_pdb(const char *path, float temperature_k, int step, double potential, const float *xyz) const;
 
     cgppd_engine *engine_ = nullptr;
     FILE *fractionBoundFile = nullptr, *boundConformationsFile = nullptr, *acceptanceRatioFile = nullptr,

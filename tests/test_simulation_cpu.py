@@ -160,3 +160,60 @@ def test_pdb_reader(tmp_path, refdata, case):
         assert n == -1 and expect in msg
     finally:
         L.cgppd_aminoacids_destroy(a)
+
+
+def write_sample(path, aa_handle, title, temperature, sample, potential, xyz, types, seq, chain, mol):
+    import numpy as np
+    L = cgppd_gb300.lib()
+    f = L.cgppd_pdb_write_sample
+    f.restype = ctypes.c_int
+    P = ctypes.POINTER
+    f.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_float, ctypes.c_int, ctypes.c_double,
+                  ctypes.c_int, P(ctypes.c_float), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]
+    arrs = [np.ascontiguousarray(x, np.int32) for x in (types, seq, chain, mol)]
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    return f(str(path).encode(), aa_handle, title.encode(), temperature, sample, potential, len(arrs[0]),
+             xyz.ctypes.data_as(P(ctypes.c_float)), *[x.ctypes.data_as(P(ctypes.c_int)) for x in arrs])
+
+
+def test_sample_pdb_layout_matches_reference(tmp_path, refdata):
+    # Replica::saveAsSinglePDB (src/Replica.cpp:1124-1168) for the reference's regression
+    # system (ubiquitin, then the UIM: replica-wide chains A and B): the layout of the
+    # reference's own sample file (tests/remctest_CPU.tgz, coordinates and header values
+    # masked), and the header values as the reference prints them
+    import numpy as np
+    from helpers import write_reference_data_dir
+    write_reference_data_dir(str(tmp_path), refdata)
+    L = cgppd_gb300.lib()
+    a = L.cgppd_aminoacids_create()
+    d = tmp_path / "data"
+    assert L.cgppd_aminoacids_load(a, str(d / "AminoAcids").encode(), str(d / "pair_potentials_MJ1996").encode()) == 0
+    parts = [read_pdb(d / "application" / name, a)[1] for name in ("ubq.pdb", "uim.pdb")]
+    types, seq, chain, mol, xyz = [], [], [], [], []
+    base = 0
+    for k, r in enumerate(parts):
+        types += list(r["types"])
+        seq += list(r["seq"])
+        chain += [base + c for c in r["chain_index"]]
+        mol += [k] * len(r["types"])
+        xyz.append(r["xyz"])
+        base += r["num_chains"]
+    out = tmp_path / "sample_0_240.0K_-0.00.pdb"
+    pot = 50.3998794556
+    assert write_sample(out, a, "remctest_0", 240.0, 0, pot, np.concatenate(xyz), types, seq, chain, mol) == 0
+    lines = out.read_text().splitlines()
+
+    def mask(ln):  # tests/golden/make_golden.py
+        if ln.startswith("ATOM"):
+            return ln[:30] + "*" + ln[54:]
+        if ln.startswith("REMARK") and ":" in ln and not ln.startswith("REMARK simulation"):
+            return ln.split(":")[0] + ":*"
+        return ln
+    assert [mask(ln) for ln in lines] == refdata["remctest"]["CPU"]["pdb_sample_layout"]
+    assert lines[1:4] == ["REMARK temperature: 240.0 ", "REMARK sample: 0 ",
+                          "REMARK potential: %0.10f " % float(np.float32(pot))]
+    first = np.concatenate(xyz)[0]
+    assert lines[4][30:54] == "%8.3f%8.3f%8.3f" % tuple(float(v) for v in first)
+    # bad input is refused with a message
+    assert write_sample(out, a, "t", 300.0, 0, 0.0, np.zeros((1, 3)), [25], [1], [0], [0]) == -1
+    L.cgppd_aminoacids_destroy(a)
