@@ -561,7 +561,12 @@ void Simulation::run()
     const int per_block = freq > 0 ? (K + freq - 1) / freq : 0;
     int chunk = RE;
     if (per_block > 0) {
-        chunk = std::max(1, std::min(RE, 4096 / per_block));
+        // records per replica held between reads: at most 4096, and the samples'
+        // coordinates within 256 MB, but always one block's
+        const long long per_record = (long long)parameters.replicas * sample_residues() * 16;
+        const long long fit = per_record > 0 ? (256LL << 20) / per_record : 4096;
+        const int records = std::max(per_block, (int)std::min<long long>(4096, fit));
+        chunk = std::max(1, std::min(RE, records / per_block));
         if (cgppd_engine_set_sample_snapshots(engine_, sample_residues()) != 0 ||
             cgppd_engine_set_sample_log(engine_, chunk * per_block) != 0)
             throw "MC run failed.";
